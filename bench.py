@@ -1,0 +1,371 @@
+"""Benchmark: Barnes-Hut self accelerations of a 1,000,000-particle Plummer
+sphere (theta=0.5, softening=0.01, G=1, leaf_size=32) on one GB300.
+
+One step = one full solve through a persistent tree handle: bounding box,
+Morton keys, radix sort, gather, bottom-up node moments, and the traversal
+over all N targets (what bhut.Tree.rebuild + Tree.accelerations do), with
+inputs already resident in HBM.  ``e2e`` repeats the metric through the
+public API (``bhut_gb300.accelerations``) with host NumPy buffers, so the
+host<->device copies are inside its timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--form exact|fast|fp32]
+    python bench.py --impl reference ...   # the reference's algorithm on the host cores
+
+Under torchrun (N > 1) every rank solves its own system (replicas; the
+path has no exchange step), times are maxed over ranks and rank 0 prints
+one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "accels/s N=1M θ=0.5; served solves/s & p99 vs plain GPU at equal FP64 err"
+N_DEFAULT = 1_000_000
+THETA, EPS, G, LEAF = 0.5, 0.01, 1.0, 32
+FLOPS_PER_INTERACTION = 20  # conventional N-body count per pair/monopole evaluation
+
+
+def _workload_desc(n, form):
+    return {
+        "workload": f"Plummer sphere N={n:,} (a=1, radii truncated at 20a, equal masses 1/N, "
+                    f"seed 1+rank), self accelerations: tree build + Barnes-Hut traversal",
+        "n": n, "theta": THETA, "softening": EPS, "G": G, "leaf_size": LEAF, "form": form,
+        "l2": "512 MiB buffer written between timed steps (L2 flush)",
+    }
+
+
+# ---------------------------------------------------------------------------
+# process group (replicas only: barrier + max of times, no data-path traffic)
+# ---------------------------------------------------------------------------
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int = 0):
+        self.dev = device_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle (scalar FP64 restatement of the reference's path)
+# ---------------------------------------------------------------------------
+def cpu_solve_sample(pos, m, sample_targets: int, seed: int = 0) -> dict:
+    """Times the oracle on the host: full tree build (serial, as the
+    reference's build) plus the traversal of a bounded random sample of
+    targets on all host threads; returns the extrapolated whole-job rate."""
+    from oracle import oracle
+    n = len(pos)
+    t0 = time.perf_counter()
+    tree = oracle.build_tree(pos, m, LEAF)
+    t_build = time.perf_counter() - t0
+    idx = np.random.default_rng(seed).choice(n, min(sample_targets, n), replace=False)
+    t0 = time.perf_counter()
+    oracle.accelerations(tree, pos, m, theta=THETA, softening=EPS, G=G, self_index=idx)
+    t_trav = time.perf_counter() - t0
+    per_target = t_trav / len(idx)
+    total = t_build + per_target * n
+    return {"value": n / total, "t_build_s": t_build, "t_sample_s": t_trav,
+            "sample_targets": len(idx), "cores": oracle.num_threads()}
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the reference's algorithm (oracle port, C, OpenMP on
+    every host core) on the same workload; rank 0 only."""
+    if rank != 0:
+        return
+    from bhut_gb300 import workloads
+    from oracle import oracle
+    oracle.build()
+    pos, m = workloads.plummer(args.n, seed=1)
+    sample = args.ref_sample
+    # calibrate the sample so that one step stays near 2 s of traversal
+    probe = cpu_solve_sample(pos, m, 512, seed=99)
+    rate = probe["sample_targets"] / max(probe["t_sample_s"], 1e-9)
+    if sample <= 0:
+        sample = int(min(args.n, max(1024, rate * 2.0)))
+    for w in range(args.warmup):
+        cpu_solve_sample(pos, m, sample, seed=w)
+    vals, build_s = [], []
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        r = cpu_solve_sample(pos, m, sample, seed=100 + k)
+        vals.append(r["value"])
+        build_s.append(r["t_build_s"])
+    wall = time.perf_counter() - t0
+    value = float(statistics.mean(vals))
+    cores = oracle.num_threads()
+    desc = (f"per step: full serial tree build of N={args.n:,} plus the traversal of {sample} "
+            f"random targets on {cores} threads; accels/s = N / (build time + N x per-target "
+            f"traversal time)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "accels/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * wall / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": _workload_desc(args.n, "oracle-port"),
+        "cpu_baseline": {"value": value, "unit": "accels/s", "cores": cores, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": value, "unit": "accels/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "build_s_mean": float(statistics.mean(build_s)),
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+def measure_fp64_peak(torch) -> float:
+    """Measured FP64 throughput of this GPU: cuBLAS DGEMM (torch.matmul on
+    float64), best of 5, TFLOP/s."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    import bhut_gb300 as bh
+    from bhut_gb300 import _lib, workloads
+    from bhut_gb300.api import _Handle
+
+    torch.cuda.set_device(local)
+    L = _lib.load()
+    n = args.n
+    pos, m = workloads.plummer(n, seed=1 + rank)
+    pos_d = torch.from_numpy(pos).cuda()
+    m_d = torch.from_numpy(m).cuda()
+    out_d = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    h = _Handle(3, LEAF, stream=stream.cuda_stream)
+    h.set_form(args.form)
+
+    def step():
+        h.rebuild(pos_d, m_d)
+        ev_mid = torch.cuda.Event(enable_timing=True)
+        ev_mid.record(stream)
+        h.accel_self(THETA, EPS, G, out_d)
+        return ev_mid
+
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    p2p, m2p, visits = h.stats()
+
+    clocks = ClockSampler(local)
+    _barrier(ws)
+    torch.cuda.synchronize()
+    clocks.start()
+    launches0 = L.bhut_launch_count()
+    total_ms, trav_ms = 0.0, 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        mid = step()
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        trav_ms += mid.elapsed_time(e1)
+    torch.cuda.synchronize()
+    launches = L.bhut_launch_count() - launches0
+    clk = clocks.stop()
+    _barrier(ws)
+    t_max = _max_over_ranks(total_ms / 1e3, ws)
+    value = ws * n * args.steps / t_max
+
+    # end to end through the public API with host buffers
+    e2e_steps = max(1, args.e2e_steps)
+    bh.accelerations(pos, m, theta=THETA, softening=EPS, G=G, leaf_size=LEAF, form=args.form)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        acc = bh.accelerations(pos, m, theta=THETA, softening=EPS, G=G, leaf_size=LEAF,
+                               form=args.form)
+    torch.cuda.synchronize()
+    t_e2e = _max_over_ranks(time.perf_counter() - t0, ws)
+    e2e_value = ws * n * e2e_steps / t_e2e
+    assert np.all(np.isfinite(acc))
+
+    if rank != 0:
+        h.close()
+        return
+    peak = measure_fp64_peak(torch)
+    trav_s = trav_ms / 1e3 / args.steps
+    flops = FLOPS_PER_INTERACTION * (p2p + m2p)
+    achieved = flops / trav_s / 1e12
+    traffic = _traffic_from_profile(args)
+    line = {
+        "metric": METRIC, "value": value, "unit": "accels/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": _workload_desc(n, args.form),
+        "e2e": {"value": e2e_value, "unit": "accels/s",
+                "h2d_bytes_per_step": int(pos.nbytes + m.nbytes),
+                "d2h_bytes_per_step": int(n * 3 * 8), "api": "bhut_gb300.accelerations"},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "fp64", "kernel": "k_traverse_exact" if args.form == "exact"
+                     else f"traversal ({args.form})",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 pipe; "
+                                    "MEASURED_PEAKS.json has no FP64 figure)",
+                     "flops_per_launch": flops,
+                     "flop_rule": f"{FLOPS_PER_INTERACTION} x (pair + monopole evaluations) "
+                                  "counted by the kernel"},
+        "traversal_ms": trav_s * 1e3,
+        "build_ms": (total_ms - trav_ms) / args.steps,
+        "interactions_per_solve": {"p2p": p2p, "m2p": m2p, "node_visits": visits},
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        cb = cpu_solve_sample(pos, m, args.cpu_sample)
+        line["cpu_baseline"] = {
+            "value": cb["value"], "unit": "accels/s", "cores": cb["cores"], "kind": "port",
+            "sample": f"oracle (C restatement of the reference's path): full serial build of "
+                      f"N={n:,} ({cb['t_build_s']:.2f} s) + traversal of "
+                      f"{cb['sample_targets']} random targets ({cb['t_sample_s']:.2f} s, "
+                      f"{cb['cores']} threads), extrapolated to N targets"}
+    h.close()
+    print(json.dumps(line), flush=True)
+
+
+def _traffic_from_profile(args):
+    """DRAM bytes per traversal launch from the committed ncu summary, if any."""
+    path = os.path.join(HERE, "profiles", f"traversal_{args.form}_dram.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get("dram_bytes_per_launch_scaled")
+    except (OSError, ValueError):
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--form", choices=["exact", "fast", "fp32"], default=None)
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--ref-sample", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.form is None:
+        from bhut_gb300.api import DEFAULT_FORM
+        args.form = DEFAULT_FORM
+    ws, rank, local = _dist()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

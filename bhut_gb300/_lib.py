@@ -1,0 +1,100 @@
+"""ctypes binding of libbhut_gb300.so (the C ABI in include/bhut_gb300.h).
+
+The library must have been built (``python -m bhut_gb300._build`` or
+``__graft_entry__.build()``); importing the engine without it fails loudly --
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_build", "libbhut_gb300.so")
+
+BHUT_OK = 0
+BHUT_EINVAL = 1
+BHUT_ENOTBUILT = 2
+BHUT_ECUDA = 3
+BHUT_ENOMEM = 4
+BHUT_EDEVICE = 5
+BHUT_EINTERNAL = 6
+
+FORM_EXACT = 0
+FORM_FAST = 1
+FORM_FP32 = 2
+FORMS = {"exact": FORM_EXACT, "fast": FORM_FAST, "fp32": FORM_FP32}
+
+_VP = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+_INT = ctypes.c_int
+
+# name -> (restype, argtypes); every symbol here is declared in the header
+SIGNATURES = {
+    "bhut_version": (ctypes.c_char_p, []),
+    "bhut_last_error": (_INT, [ctypes.c_char_p, ctypes.c_size_t]),
+    "bhut_tree_create": (_INT, [_INT, _INT, _VP, ctypes.POINTER(_VP)]),
+    "bhut_tree_build": (_INT, [_VP, _VP, _VP, _I64]),
+    "bhut_tree_refit": (_INT, [_VP, _VP, _VP, _I64, ctypes.POINTER(_INT)]),
+    "bhut_tree_rebuild": (_INT, [_VP, _VP, _VP, _I64]),
+    "bhut_tree_accel_self": (_INT, [_VP, _D, _D, _D, _VP]),
+    "bhut_tree_accel_targets": (_INT, [_VP, _VP, _I64, _D, _D, _D, _VP]),
+    "bhut_tree_set_form": (_INT, [_VP, _INT]),
+    "bhut_tree_info": (_INT, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
+                              ctypes.POINTER(_INT), ctypes.POINTER(_INT)]),
+    "bhut_tree_export": (_INT, [_VP] * 11),
+    "bhut_tree_destroy": (None, [_VP]),
+    "bhut_tree_stats": (_INT, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
+                               ctypes.POINTER(_I64)]),
+    "bhut_launch_count": (ctypes.c_longlong, []),
+    "bhut_morton_keys": (_INT, [_VP, _I64, _INT, _VP, _VP]),
+    "bhut_morton_argsort": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),
+    "bhut_direct_accelerations": (_INT, [_VP, _VP, _I64, _INT, _VP, _I64, _D, _D, _VP, _VP]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+class EngineError(RuntimeError):
+    """A CUDA-side failure reported by the engine."""
+
+
+def load():
+    """Load the shared library and bind every C-ABI entry point."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build the CUDA engine first "
+                "(python -m bhut_gb300._build, or __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+        return L
+
+
+def last_error() -> str:
+    L = load()
+    buf = ctypes.create_string_buffer(1024)
+    L.bhut_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(status: int) -> None:
+    """Map a C-ABI status to the exception type the reference raises."""
+    if status == BHUT_OK:
+        return
+    msg = last_error()
+    if status in (BHUT_EINVAL, BHUT_ENOTBUILT):
+        raise ValueError(msg)
+    if status == BHUT_ENOMEM:
+        raise MemoryError(msg)
+    raise EngineError(msg)

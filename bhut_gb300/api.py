@@ -1,0 +1,534 @@
+"""Public API: a drop-in for bhut 0.1.0's ``accelerations`` and ``Tree``.
+
+Signatures, argument meaning, validation order and error messages follow
+bhut/api.py (file:line cited per function).  The arithmetic runs in
+libbhut_gb300.so through the C ABI of include/bhut_gb300.h; this module only
+validates, converts and marshals.  Inputs may be anything ``np.asarray``
+accepts, or torch tensors: CUDA tensors are passed to the engine zero-copy
+and the result comes back as a CUDA tensor on the same device.
+
+One keyword is added to both entry points: ``form`` selects the traversal
+arithmetic -- ``"exact"`` (FP64; pair terms bit-identical to the reference's
+Numba loop), ``"fast"`` (FP64-accurate float-float arithmetic on the FP32
+pipe) or ``"fp32"`` (the FP32/Kahan precision form).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Any, Optional
+
+import numpy as np
+
+from . import _lib
+
+DEFAULT_FORM = "exact"
+
+
+# ---------------------------------------------------------------------------
+# array plumbing
+# ---------------------------------------------------------------------------
+def _is_torch(x) -> bool:
+    return type(x).__module__.split(".")[0] == "torch" and hasattr(x, "data_ptr")
+
+
+def _is_cuda_tensor(x) -> bool:
+    return _is_torch(x) and bool(getattr(x, "is_cuda", False))
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _ptr(a) -> Optional[int]:
+    if a is None:
+        return None
+    if _is_torch(a):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+def _sync_torch(*arrays) -> None:
+    if any(_is_cuda_tensor(a) for a in arrays if a is not None):
+        _torch().cuda.current_stream().synchronize()
+
+
+def _to_f64(x):
+    """np.asarray(x, dtype=float64), keeping CUDA tensors on their device."""
+    if _is_cuda_tensor(x):
+        t = x.detach()
+        if t.dtype != _torch().float64:
+            t = t.to(_torch().float64)
+        return t.contiguous()
+    return np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+
+
+def _shape(a):
+    return tuple(a.shape)
+
+
+def _empty_like_out(ref, shape):
+    if _is_cuda_tensor(ref):
+        return _torch().empty(shape, dtype=_torch().float64, device=ref.device)
+    return np.empty(shape, dtype=np.float64)
+
+
+# ---------------------------------------------------------------------------
+# validation (bhut/api.py:84-152, bhut/backends/base.py:102-166)
+# ---------------------------------------------------------------------------
+def _validate_dimensions(dim: int) -> None:
+    if dim not in (2, 3):
+        raise ValueError(f"dim must be 2 or 3, got {dim}")
+
+
+def _check_backend(array, backend: str) -> str:
+    """get_namespace (bhut/backends/base.py:102-166) without the Dask path."""
+    if not _is_cuda_tensor(array):
+        np.asarray(array)
+    if backend == "auto":
+        return "numpy"
+    if backend == "numpy":
+        return "numpy"
+    if backend == "dask":
+        raise ValueError("Unsupported backend: dask. The Dask chunking path is not part of the "
+                         "GB300 engine; pass NumPy arrays or torch tensors")
+    raise ValueError(f"Unsupported backend: {backend}. Supported: 'numpy', 'dask', 'auto'")
+
+
+def _validate_accelerations_inputs(positions, masses, *, dim, softening, theta, G, leaf_size):
+    """bhut/api.py:90-152."""
+    _validate_dimensions(dim)
+    positions = _to_f64(positions)
+    masses = _to_f64(masses)
+    if len(_shape(positions)) != 2:
+        raise ValueError(f"positions must be 2D array, got shape {_shape(positions)}")
+    if len(_shape(masses)) != 1:
+        raise ValueError(f"masses must be 1D array, got shape {_shape(masses)}")
+    N, actual_dim = _shape(positions)
+    if actual_dim != dim:
+        raise ValueError(f"positions has {actual_dim} dimensions but dim={dim}")
+    if _shape(masses)[0] != N:
+        raise ValueError(f"positions has {N} particles but masses has {_shape(masses)[0]} elements")
+    if np.isscalar(softening):
+        softening = float(softening)
+        if softening < 0:
+            raise ValueError(f"softening must be non-negative, got {softening}")
+    else:
+        softening = _host(softening)
+        if len(softening.shape) != 1:
+            raise ValueError(f"softening array must be 1D, got shape {softening.shape}")
+        if softening.shape[0] != N:
+            raise ValueError(f"softening array has {softening.shape[0]} elements but need {N}")
+        if np.any(softening < 0):
+            raise ValueError("all softening values must be non-negative")
+    if theta < 0:
+        raise ValueError(f"theta must be non-negative, got {theta}")
+    if leaf_size <= 0:
+        raise ValueError(f"leaf_size must be positive, got {leaf_size}")
+    return positions, masses, softening
+
+
+def _host(x) -> np.ndarray:
+    if _is_torch(x):
+        return x.detach().cpu().numpy().astype(np.float64)
+    return np.asarray(x, dtype=np.float64)
+
+
+def _scalar_softening(softening, n: int) -> float:
+    """evaluate_accelerations (bhut/api.py:400-418): uniform arrays collapse to
+    a scalar, anything else is rejected."""
+    s = np.asarray(_host(softening) if _is_torch(softening) else softening, dtype=np.float64)
+    if s.ndim > 1:
+        raise ValueError("Softening must be scalar or 1D array")
+    if s.ndim == 1 and len(s) != n:
+        raise ValueError("Softening array length must match number of particles")
+    if np.any(s < 0):
+        raise ValueError("Softening must be non-negative")
+    if s.ndim == 1:
+        if not np.allclose(s, s[0]):
+            raise ValueError("Variable softening per particle not yet implemented")
+        return float(s[0])
+    return float(s)
+
+
+def _form_code(form: str) -> int:
+    try:
+        return _lib.FORMS[form]
+    except KeyError:
+        raise ValueError(f"form must be one of {sorted(_lib.FORMS)}, got {form!r}") from None
+
+
+# ---------------------------------------------------------------------------
+# TreeData export (bhut/tree/node.py:15-77)
+# ---------------------------------------------------------------------------
+@dataclass
+class TreeData:
+    """Host copy of the device tree with the reference's TreeData fields."""
+
+    center: np.ndarray
+    half_size: np.ndarray
+    mass: np.ndarray
+    com: np.ndarray
+    first_child: np.ndarray
+    child_count: np.ndarray
+    start: np.ndarray
+    count: np.ndarray
+    is_leaf: np.ndarray
+    perm: np.ndarray
+    dim: int
+    leaf_size: int
+
+    @property
+    def num_nodes(self) -> int:
+        return len(self.center)
+
+    @property
+    def num_particles(self) -> int:
+        return len(self.perm)
+
+    def get_children(self, node_idx: int) -> np.ndarray:
+        if self.is_leaf[node_idx]:
+            return np.array([], dtype=np.intp)
+        first = self.first_child[node_idx]
+        return np.arange(first, first + self.child_count[node_idx], dtype=np.intp)
+
+    def get_particles(self, node_idx: int) -> np.ndarray:
+        s = self.start[node_idx]
+        return self.perm[np.arange(s, s + self.count[node_idx], dtype=np.intp)]
+
+
+class _Handle:
+    """Owns one bhut_tree* of the C ABI."""
+
+    def __init__(self, dim: int, leaf_size: int, stream: int | None = None):
+        self.L = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(self.L.bhut_tree_create(int(dim), int(leaf_size), stream, ctypes.byref(h)))
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.L.bhut_tree_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_form(self, form: str) -> None:
+        _lib.check(self.L.bhut_tree_set_form(self.h, _form_code(form)))
+
+    def build(self, pos, m) -> None:
+        _sync_torch(pos, m)
+        _lib.check(self.L.bhut_tree_build(self.h, _ptr(pos), _ptr(m), int(_shape(pos)[0])))
+
+    def refit(self, pos, m) -> bool:
+        _sync_torch(pos, m)
+        rebuilt = ctypes.c_int(0)
+        _lib.check(self.L.bhut_tree_refit(self.h, _ptr(pos), _ptr(m), int(_shape(pos)[0]),
+                                          ctypes.byref(rebuilt)))
+        return bool(rebuilt.value)
+
+    def rebuild(self, pos, m) -> None:
+        _sync_torch(pos, m)
+        _lib.check(self.L.bhut_tree_rebuild(self.h, _ptr(pos), _ptr(m), int(_shape(pos)[0])))
+
+    def stats(self):
+        """(pair evaluations, monopole evaluations, node visits) of the last
+        traversal, summed over targets."""
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(self.L.bhut_tree_stats(self.h, ctypes.byref(a), ctypes.byref(b),
+                                          ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def info(self):
+        n, m = ctypes.c_int64(), ctypes.c_int64()
+        d, L = ctypes.c_int(), ctypes.c_int()
+        _lib.check(self.L.bhut_tree_info(self.h, ctypes.byref(n), ctypes.byref(m), ctypes.byref(d),
+                                         ctypes.byref(L)))
+        return n.value, m.value, d.value, L.value
+
+    def accel_self(self, theta, eps, G, out) -> None:
+        _sync_torch(out)
+        _lib.check(self.L.bhut_tree_accel_self(self.h, float(theta), float(eps), float(G),
+                                               _ptr(out)))
+
+    def accel_targets(self, targets, theta, eps, G, out) -> None:
+        _sync_torch(targets, out)
+        _lib.check(self.L.bhut_tree_accel_targets(self.h, _ptr(targets), int(_shape(targets)[0]),
+                                                  float(theta), float(eps), float(G), _ptr(out)))
+
+    def export(self) -> TreeData:
+        n, m, dim, L = self.info()
+        center = np.empty((m, dim))
+        half = np.empty(m)
+        mass = np.empty(m)
+        com = np.empty((m, dim))
+        fc = np.empty(m, np.int64)
+        cc = np.empty(m, np.int64)
+        st = np.empty(m, np.int64)
+        ct = np.empty(m, np.int64)
+        il = np.empty(m, np.uint8)
+        perm = np.empty(n, np.int64)
+        _lib.check(self.L.bhut_tree_export(self.h, *[a.ctypes.data for a in
+                                                      (center, half, mass, com, fc, cc, st, ct, il,
+                                                       perm)]))
+        return TreeData(center, half, mass, com, fc.astype(np.intp), cc.astype(np.intp),
+                        st.astype(np.intp), ct.astype(np.intp), il.astype(bool),
+                        perm.astype(np.intp), dim, L)
+
+
+# ---------------------------------------------------------------------------
+# functional API (bhut/api.py:254-364)
+# ---------------------------------------------------------------------------
+def accelerations(
+    positions,
+    masses,
+    *,
+    theta: float = 0.5,
+    softening: Any = 0.0,
+    G: float = 1.0,
+    dim: int = 3,
+    backend: str = "auto",
+    leaf_size: int = 32,
+    criterion: str = "bh",
+    multipole: str = "mono",
+    form: str | None = None,
+):
+    """Gravitational self-accelerations with the Barnes-Hut algorithm.
+
+    Same contract as bhut.accelerations (bhut/api.py:254-364): builds the
+    Morton count-split tree of the particles and evaluates the softened
+    monopole/P2P traversal at every particle, skipping self-interaction.
+    Returns a float64 (N, dim) array (a CUDA tensor for CUDA tensor input).
+    """
+    if criterion != "bh":
+        raise ValueError(f"criterion must be 'bh', got '{criterion}'")
+    if multipole != "mono":
+        raise ValueError(f"multipole must be 'mono', got '{multipole}'")
+    _check_backend(positions, backend)
+    positions, masses, softening = _validate_accelerations_inputs(
+        positions, masses, dim=dim, softening=softening, theta=theta, G=G, leaf_size=leaf_size)
+    n = _shape(positions)[0]
+    if n == 0:
+        raise ValueError("Cannot build tree with zero particles")
+    eps = _scalar_softening(softening, n)
+    if theta < 0:
+        raise ValueError("Opening angle theta must be non-negative")
+    h = _Handle(dim, leaf_size)
+    try:
+        h.set_form(form or DEFAULT_FORM)
+        h.build(positions, masses)
+        out = _empty_like_out(positions, (n, dim))
+        h.accel_self(theta, eps, G, out)
+    finally:
+        h.close()
+    return out
+
+
+def build_tree(positions, masses, *, leaf_size: int, backend: str, dim: int) -> TreeData:
+    """bhut/api.py:155-191: build and return the TreeData arrays."""
+    _check_backend(positions, backend)
+    positions = _to_f64(positions)
+    masses = _to_f64(masses)
+    h = _Handle(dim, leaf_size)
+    try:
+        h.build(positions, masses)
+        return h.export()
+    finally:
+        h.close()
+
+
+# ---------------------------------------------------------------------------
+# object API (bhut/api.py:432-786)
+# ---------------------------------------------------------------------------
+class Tree:
+    """Barnes-Hut tree resident in GPU memory (bhut/api.py:432-786).
+
+    Attributes as in the reference: ``positions``, ``masses``, ``dim``,
+    ``leaf_size``, ``backend``, ``_tree`` (TreeData, exported from the device
+    on access) and ``_is_built``.
+    """
+
+    def __init__(self, positions, masses, *, leaf_size: int = 32, backend: str = "auto",
+                 dim: int = 3, form: str | None = None):
+        _validate_dimensions(dim)
+        self.positions, self.masses, _ = _validate_accelerations_inputs(
+            positions, masses, dim=dim, softening=0.0, theta=0.5, G=1.0, leaf_size=leaf_size)
+        self.dim = dim
+        self.leaf_size = leaf_size
+        self.backend = backend
+        self._is_built = False
+        self._tree_cache: TreeData | None = None
+        self._handle: _Handle | None = None
+        self._form = form or DEFAULT_FORM
+        _form_code(self._form)
+        _check_backend(self.positions, backend)
+
+    # -- reference attribute ``_tree``: None until built --------------------
+    @property
+    def _tree(self) -> TreeData | None:
+        if not self._is_built or self._handle is None:
+            return None
+        if self._tree_cache is None:
+            self._tree_cache = self._handle.export()
+        return self._tree_cache
+
+    @_tree.setter
+    def _tree(self, value) -> None:
+        if value is None:
+            self._is_built = False
+            self._tree_cache = None
+        else:
+            raise AttributeError("_tree is derived from the device tree")
+
+    def close(self) -> None:
+        """Release the device memory of this tree."""
+        if self._handle is not None:
+            self._handle.close()
+            self._handle = None
+        self._is_built = False
+        self._tree_cache = None
+
+    def set_form(self, form: str) -> "Tree":
+        _form_code(form)
+        self._form = form
+        return self
+
+    def build(self) -> "Tree":
+        """bhut/api.py:497-511."""
+        if _shape(self.positions)[0] == 0:
+            raise ValueError("Cannot build tree with zero particles")
+        if self._handle is None:
+            self._handle = _Handle(self.dim, self.leaf_size)
+        self._tree_cache = None
+        self._is_built = False
+        self._handle.build(self.positions, self.masses)
+        self._is_built = True
+        return self
+
+    def refit(self, new_positions, new_masses=None) -> "Tree":
+        """bhut/api.py:513-562 (falls back to rebuild as refit.py:195-251)."""
+        if not self._is_built or self._handle is None:
+            raise ValueError("Tree must be built before refitting. Call build() first.")
+        if new_masses is None:
+            new_masses = self.masses
+        new_positions, new_masses, _ = _validate_accelerations_inputs(
+            new_positions, new_masses, dim=self.dim, softening=0.0, theta=0.5, G=1.0,
+            leaf_size=self.leaf_size)
+        if _shape(new_positions)[0] == 0:
+            raise ValueError("Cannot build tree with zero particles")
+        self._tree_cache = None
+        self._handle.refit(new_positions, new_masses)
+        self.positions = new_positions
+        self.masses = new_masses
+        return self
+
+    def rebuild(self, new_positions, new_masses=None) -> "Tree":
+        """bhut/api.py:564-606."""
+        if new_masses is None:
+            new_masses = self.masses
+        new_positions, new_masses, _ = _validate_accelerations_inputs(
+            new_positions, new_masses, dim=self.dim, softening=0.0, theta=0.5, G=1.0,
+            leaf_size=self.leaf_size)
+        self.positions = new_positions
+        self.masses = new_masses
+        self._is_built = False
+        self._tree_cache = None
+        return self.build()
+
+    def accelerations(self, targets=None, *, theta: float = 0.5, softening: Any = 0.0,
+                      G: float = 1.0):
+        """bhut/api.py:608-688: self accelerations, or at external targets."""
+        if not self._is_built:
+            raise ValueError("Tree must be built before evaluating accelerations")
+        if targets is None:
+            return self.evaluate_accelerations(softening, theta, G)
+        targets = _to_f64(targets)
+        if len(_shape(targets)) != 2:
+            raise ValueError(f"targets must be 2D array, got shape {_shape(targets)}")
+        if _shape(targets)[1] != self.dim:
+            raise ValueError(f"targets has {_shape(targets)[1]} dimensions but tree has {self.dim}")
+        M = _shape(targets)[0]
+        if not np.isscalar(softening):
+            s = _host(softening)
+            if s.shape != (M,):
+                raise ValueError(f"softening array shape {s.shape} does not match "
+                                 f"targets shape ({M},)")
+            eps = _scalar_softening(s, M)
+        else:
+            eps = float(softening)
+            if eps < 0:
+                raise ValueError(f"softening must be non-negative, got {eps}")
+        if theta < 0:
+            raise ValueError(f"theta must be non-negative, got {theta}")
+        out = _empty_like_out(targets, (M, self.dim))
+        if M:
+            self._handle.set_form(self._form)
+            self._handle.accel_targets(targets, theta, eps, G, out)
+        return out
+
+    def evaluate_accelerations(self, softening, theta: float = 0.5, G: float = 1.0):
+        """bhut/api.py:733-786."""
+        if not self._is_built or self._handle is None:
+            raise RuntimeError("Tree not built. Call build() first.")
+        if not isinstance(softening, (int, float)):
+            raise ValueError("Only scalar softening is currently supported")
+        if softening < 0:
+            raise ValueError("Softening must be non-negative")
+        if theta < 0:
+            raise ValueError("Opening angle theta must be non-negative")
+        n = _shape(self.positions)[0]
+        out = _empty_like_out(self.positions, (n, self.dim))
+        self._handle.set_form(self._form)
+        self._handle.accel_self(theta, float(softening), G, out)
+        return out
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# building blocks exposed for parity checks
+# ---------------------------------------------------------------------------
+def morton_keys(positions) -> np.ndarray:
+    """Morton keys in input order (bbox.py + morton.py:48-102)."""
+    pos = _to_f64(positions)
+    n, dim = _shape(pos)
+    keys = np.empty(n, np.uint64)
+    _sync_torch(pos)
+    _lib.check(_lib.load().bhut_morton_keys(_ptr(pos), n, dim, keys.ctypes.data, None))
+    return keys
+
+
+def morton_argsort(positions):
+    """(sorted keys, stable permutation) as sort_by_morton (morton.py:105-147)."""
+    pos = _to_f64(positions)
+    n, dim = _shape(pos)
+    keys = np.empty(n, np.uint64)
+    perm = np.empty(n, np.int64)
+    _sync_torch(pos)
+    _lib.check(_lib.load().bhut_morton_argsort(_ptr(pos), n, dim, keys.ctypes.data,
+                                               perm.ctypes.data, None))
+    return keys, perm
+
+
+def direct_accelerations(positions, masses, *, softening: float = 0.0, G: float = 1.0,
+                         targets=None):
+    """FP64 direct sum on the GPU (self accelerations when targets is None)."""
+    pos = _to_f64(positions)
+    m = _to_f64(masses)
+    n, dim = _shape(pos)
+    tg = None if targets is None else _to_f64(targets)
+    mt = n if tg is None else _shape(tg)[0]
+    out = _empty_like_out(pos, (mt, dim))
+    _sync_torch(pos, m, tg, out)
+    _lib.check(_lib.load().bhut_direct_accelerations(_ptr(pos), _ptr(m), n, dim, _ptr(tg), mt,
+                                                     float(softening), float(G), _ptr(out), None))
+    return out

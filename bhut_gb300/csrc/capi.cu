@@ -1,0 +1,628 @@
+// C ABI of the engine (include/bhut_gb300.h): tree handles, host/device
+// pointer staging, and the build / refit / traversal pipelines.
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/bhut_gb300.h"
+#include "tree.cuh"
+
+namespace bhut {
+
+// ---- error reporting --------------------------------------------------------
+static thread_local std::string g_last_error;
+
+void set_error(const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+static std::atomic<long long> g_launches{0};
+
+void note_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+int cuda_status(cudaError_t e, const char* what)
+{
+    set_error("CUDA error %s (%s) in %s", cudaGetErrorName(e), cudaGetErrorString(e), what);
+    return e == cudaErrorMemoryAllocation ? kNoMemory : kCuda;
+}
+
+// ---- device buffers -----------------------------------------------------------
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t need, cudaStream_t s)
+    {
+        if (need <= bytes && p) return kOk;
+        if (p) {
+            BHUT_CUDA(cudaFreeAsync(p, s));
+            p = nullptr;
+            bytes = 0;
+        }
+        size_t want = need < 256 ? 256 : need;
+        cudaError_t e = cudaMallocAsync(&p, want, s);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return cuda_status(e, "cudaMallocAsync");
+        }
+        bytes = want;
+        return kOk;
+    }
+    void release(cudaStream_t s)
+    {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T> T* as() const { return (T*)p; }
+};
+
+bool is_device_pointer(const void* p)
+{
+    if (!p) return false;
+    cudaPointerAttributes a;
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Copies n bytes from a host or device pointer into a device buffer.
+int stage_in(DevBuf& dst, const void* src, size_t bytes, cudaStream_t s)
+{
+    BHUT_TRY(dst.ensure(bytes, s));
+    if (bytes == 0) return kOk;
+    BHUT_CUDA(cudaMemcpyAsync(dst.p, src, bytes,
+                              is_device_pointer(src) ? cudaMemcpyDeviceToDevice
+                                                     : cudaMemcpyHostToDevice, s));
+    return kOk;
+}
+
+}  // namespace bhut
+
+using namespace bhut;
+
+struct bhut_tree {
+    int dim = 3;
+    int leaf = 32;
+    int form = BHUT_FORM_EXACT;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bool built = false;
+    int64_t n = 0;
+    int64_t m = 0;
+    TopoTables tt{};
+    bool topo_valid = false;
+    // particles
+    DevBuf pos, mass, keys, perm, sx, sy, sz, sm;
+    // nodes
+    DevBuf cm, size, center, half, lo, hi, first_child, start, count, parent, leaf_list, arrive;
+    // scratch
+    DevBuf sort_scratch, box_partial, box, counters, err, stats;
+    unsigned long long last_stats[3] = {0, 0, 0};
+    // traversal targets
+    DevBuf tpos, tkeys, tperm, tx, ty, tz, tbox, out;
+
+    TreeDev dev() const
+    {
+        TreeDev t;
+        t.dim = dim;
+        t.leaf_size = leaf;
+        t.n = n;
+        t.m = m;
+        t.sx = sx.as<double>();
+        t.sy = sy.as<double>();
+        t.sz = sz.as<double>();
+        t.sm = sm.as<double>();
+        t.perm = perm.as<int32_t>();
+        t.cm = cm.as<NodeCM>();
+        t.size = size.as<double>();
+        t.first_child = first_child.as<int32_t>();
+        t.start = start.as<int32_t>();
+        t.count = count.as<int32_t>();
+        return t;
+    }
+    NodeOut nodes() const
+    {
+        return NodeOut{cm.as<NodeCM>(), size.as<double>(), center.as<double>(), half.as<double>(),
+                       lo.as<double>(), hi.as<double>()};
+    }
+};
+
+namespace {
+
+int check_err_word(bhut_tree* t, const char* what)
+{
+    unsigned e = 0;
+    BHUT_CUDA(cudaMemcpyAsync(&e, t->err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, t->stream));
+    BHUT_CUDA(cudaStreamSynchronize(t->stream));
+    if (e == 0) return kOk;
+    BHUT_CUDA(cudaMemsetAsync(t->err.p, 0, sizeof(unsigned), t->stream));
+    if (e & kErrNonFinite) {
+        set_error("positions must be finite (NaN or Inf found) in %s", what);
+        return kInvalid;
+    }
+    set_error("device error word 0x%x in %s", e, what);
+    return kDeviceFlag;
+}
+
+// Morton keys + stable sort of `n` AoS points into keys/perm (perm is the
+// sort payload, original index).  Uses the handle's scratch.
+int sort_points(bhut_tree* t, const double* dpos, int64_t n, DevBuf& keys, DevBuf& perm,
+                DevBuf& box)
+{
+    cudaStream_t s = t->stream;
+    BHUT_TRY(keys.ensure(sizeof(uint64_t) * n, s));
+    BHUT_TRY(perm.ensure(sizeof(int32_t) * n, s));
+    BHUT_TRY(box.ensure(sizeof(double) * 6, s));
+    BHUT_TRY(t->box_partial.ensure(sizeof(double) * 6 * 152 * 4, s));
+    BHUT_TRY(launch_bbox(dpos, n, t->dim, t->box_partial.as<double>(), t->counters.as<unsigned>(),
+                         box.as<double>(), t->err.as<unsigned>(), s));
+    BHUT_TRY(launch_morton(dpos, n, t->dim, box.as<double>(), keys.as<uint64_t>(),
+                           perm.as<int32_t>(), s));
+    BHUT_TRY(t->sort_scratch.ensure(sort_scratch_bytes(n), s));
+    BHUT_TRY(radix_sort_pairs(keys.as<uint64_t>(), perm.as<int32_t>(), n, t->dim == 3 ? 63 : 42,
+                              t->sort_scratch.p, s));
+    return kOk;
+}
+
+int do_build(bhut_tree* t, int64_t n)
+{
+    cudaStream_t s = t->stream;
+    const int dim = t->dim;
+    if (n != t->tt.n || !t->topo_valid) {
+        BHUT_TRY(make_topo_tables(n, t->leaf, &t->tt));
+        t->topo_valid = false;
+    }
+    t->n = n;
+    t->m = t->tt.num_nodes;
+    const int64_t m = t->m;
+    BHUT_TRY(sort_points(t, t->pos.as<double>(), n, t->keys, t->perm, t->box));
+    for (DevBuf* b : {&t->sx, &t->sy, &t->sz, &t->sm}) BHUT_TRY(b->ensure(sizeof(double) * n, s));
+    BHUT_TRY(launch_gather(t->pos.as<double>(), t->mass.as<double>(), t->perm.as<int32_t>(), n, dim,
+                           t->sx.as<double>(), t->sy.as<double>(), t->sz.as<double>(),
+                           t->sm.as<double>(), s));
+    BHUT_TRY(t->cm.ensure(sizeof(NodeCM) * m, s));
+    for (DevBuf* b : {&t->size, &t->half}) BHUT_TRY(b->ensure(sizeof(double) * m, s));
+    BHUT_TRY(t->center.ensure(sizeof(double) * m * dim, s));
+    BHUT_TRY(t->lo.ensure(sizeof(double) * m * 3, s));
+    BHUT_TRY(t->hi.ensure(sizeof(double) * m * 3, s));
+    BHUT_TRY(t->arrive.ensure(sizeof(unsigned) * m, s));
+    if (!t->topo_valid) {
+        for (DevBuf* b : {&t->first_child, &t->start, &t->count, &t->parent})
+            BHUT_TRY(b->ensure(sizeof(int32_t) * m, s));
+        BHUT_TRY(t->leaf_list.ensure(sizeof(int32_t) * t->tt.num_leaves, s));
+        BHUT_TRY(launch_topology(t->tt, t->first_child.as<int32_t>(), t->start.as<int32_t>(),
+                                 t->count.as<int32_t>(), t->parent.as<int32_t>(),
+                                 t->leaf_list.as<int32_t>(), t->counters.as<unsigned>() + 1, s));
+        t->topo_valid = true;
+    }
+    BHUT_TRY(launch_bottom_up(t->dev(), t->leaf_list.as<int32_t>(), t->tt.num_leaves,
+                              t->first_child.as<int32_t>(), t->start.as<int32_t>(),
+                              t->count.as<int32_t>(), t->parent.as<int32_t>(),
+                              t->arrive.as<unsigned>(), t->nodes(), false, nullptr, nullptr, s));
+    int st = check_err_word(t, "build");
+    if (st != kOk) {
+        t->built = false;
+        return st;
+    }
+    t->built = true;
+    return kOk;
+}
+
+int load_particles(bhut_tree* t, const double* positions, const double* masses, int64_t n)
+{
+    if (n <= 0) {
+        set_error("Cannot build tree with zero particles");
+        return kInvalid;
+    }
+    if (n > 0x7fffffffLL) {
+        set_error("at most 2^31-1 particles are supported");
+        return kInvalid;
+    }
+    if (!positions) { set_error("positions is NULL"); return kInvalid; }
+    BHUT_TRY(stage_in(t->pos, positions, sizeof(double) * n * t->dim, t->stream));
+    if (masses) {
+        BHUT_TRY(stage_in(t->mass, masses, sizeof(double) * n, t->stream));
+    } else if (n != t->n || !t->mass.p) {
+        set_error("masses are required when the particle count changes");
+        return kInvalid;
+    }
+    return kOk;
+}
+
+// Writes a device result either straight into a device out pointer or via a
+// device buffer and a copy to host memory.
+struct OutTarget {
+    double* dev;
+    double* host;
+};
+
+int out_target(bhut_tree* t, double* out, size_t bytes, OutTarget* o)
+{
+    if (is_device_pointer(out)) {
+        o->dev = out;
+        o->host = nullptr;
+        return kOk;
+    }
+    BHUT_TRY(t->out.ensure(bytes, t->stream));
+    o->dev = t->out.as<double>();
+    o->host = out;
+    return kOk;
+}
+
+int finish_out(bhut_tree* t, const OutTarget& o, size_t bytes, const char* what)
+{
+    if (o.host && bytes)
+        BHUT_CUDA(cudaMemcpyAsync(o.host, o.dev, bytes, cudaMemcpyDeviceToHost, t->stream));
+    return check_err_word(t, what);
+}
+
+int traverse(bhut_tree* t, const double* tx, const double* ty, const double* tz,
+             const int32_t* self_id, const int32_t* out_idx, int64_t nt, double theta, double eps,
+             double G, double* out)
+{
+    TreeDev d = t->dev();
+    BHUT_TRY(t->stats.ensure(sizeof(unsigned long long) * 4, t->stream));
+    BHUT_CUDA(cudaMemsetAsync(t->stats.p, 0, sizeof(unsigned long long) * 4, t->stream));
+    unsigned long long* st = t->stats.as<unsigned long long>();
+    switch (t->form) {
+    case BHUT_FORM_EXACT:
+    default:
+        BHUT_TRY(launch_traverse_exact(d, tx, ty, tz, self_id, out_idx, nt, theta, eps, G, out,
+                                       t->err.as<unsigned>(), st, t->stream));
+    }
+    BHUT_CUDA(cudaMemcpyAsync(t->last_stats, st, sizeof(unsigned long long) * 3,
+                              cudaMemcpyDeviceToHost, t->stream));
+    return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bhut_version(void) { return "bhut_gb300 0.1.0 (sm_103a)"; }
+
+int bhut_last_error(char* buf, size_t len)
+{
+    if (buf && len) {
+        size_t k = g_last_error.size() < len - 1 ? g_last_error.size() : len - 1;
+        memcpy(buf, g_last_error.data(), k);
+        buf[k] = 0;
+    }
+    return (int)g_last_error.size();
+}
+
+int bhut_tree_create(int dim, int leaf_size, void* stream, bhut_tree** out)
+{
+    if (!out) { set_error("out is NULL"); return kInvalid; }
+    *out = nullptr;
+    if (dim != 2 && dim != 3) { set_error("dim must be 2 or 3, got %d", dim); return kInvalid; }
+    if (leaf_size <= 0) { set_error("leaf_size must be positive, got %d", leaf_size); return kInvalid; }
+    bhut_tree* t = new bhut_tree();
+    t->dim = dim;
+    t->leaf = leaf_size;
+    if (stream) {
+        t->stream = (cudaStream_t)stream;
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete t; return cuda_status(e, "cudaStreamCreate"); }
+        t->own_stream = true;
+    }
+    int st = t->counters.ensure(sizeof(unsigned) * 8, t->stream);
+    if (st == kOk) st = t->err.ensure(sizeof(unsigned), t->stream);
+    if (st == kOk) {
+        cudaError_t e = cudaMemsetAsync(t->counters.p, 0, sizeof(unsigned) * 8, t->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(t->err.p, 0, sizeof(unsigned), t->stream);
+        if (e != cudaSuccess) st = cuda_status(e, "cudaMemsetAsync");
+    }
+    if (st != kOk) { bhut_tree_destroy(t); return st; }
+    *out = t;
+    return kOk;
+}
+
+int bhut_tree_build(bhut_tree* t, const double* positions, const double* masses, int64_t n)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (!masses) { set_error("masses is NULL"); return kInvalid; }
+    t->built = false;
+    BHUT_TRY(load_particles(t, positions, masses, n));
+    return do_build(t, n);
+}
+
+int bhut_tree_rebuild(bhut_tree* t, const double* positions, const double* masses, int64_t n)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    BHUT_TRY(load_particles(t, positions, masses, n));
+    t->built = false;
+    return do_build(t, n);
+}
+
+int bhut_tree_refit(bhut_tree* t, const double* positions, const double* masses, int64_t n,
+                    int* rebuilt)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (rebuilt) *rebuilt = 0;
+    if (!t->built) {
+        set_error("Tree must be built before refitting. Call build() first.");
+        return kNotBuilt;
+    }
+    if (n != t->n) {   // should_refit_vs_rebuild: different particle count
+        if (rebuilt) *rebuilt = 1;
+        return bhut_tree_rebuild(t, positions, masses, n);
+    }
+    cudaStream_t s = t->stream;
+    BHUT_TRY(load_particles(t, positions, masses, n));
+    unsigned* flag = t->counters.as<unsigned>() + 2;
+    BHUT_CUDA(cudaMemsetAsync(flag, 0, sizeof(unsigned), s));
+    BHUT_TRY(launch_outside_root(t->pos.as<double>(), n, t->dim, t->center.as<double>(),
+                                 t->half.as<double>(), flag, s));
+    unsigned outside = 0;
+    BHUT_CUDA(cudaMemcpyAsync(&outside, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    BHUT_CUDA(cudaStreamSynchronize(s));
+    if (outside) {
+        if (rebuilt) *rebuilt = 1;
+        t->built = false;
+        return do_build(t, n);
+    }
+    // refit_tree: new sorted SoA through the frozen perm, then bottom-up
+    BHUT_TRY(launch_gather(t->pos.as<double>(), t->mass.as<double>(), t->perm.as<int32_t>(), n,
+                           t->dim, t->sx.as<double>(), t->sy.as<double>(), t->sz.as<double>(),
+                           t->sm.as<double>(), s));
+    BHUT_TRY(launch_bottom_up(t->dev(), t->leaf_list.as<int32_t>(), t->tt.num_leaves,
+                              t->first_child.as<int32_t>(), t->start.as<int32_t>(),
+                              t->count.as<int32_t>(), t->parent.as<int32_t>(),
+                              t->arrive.as<unsigned>(), t->nodes(), true, t->pos.as<double>(),
+                              t->mass.as<double>(), s));
+    return check_err_word(t, "refit");
+}
+
+int bhut_tree_set_form(bhut_tree* t, int form)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (form != BHUT_FORM_EXACT) {
+        set_error("traversal form %d is not available in this build", form);
+        return kInvalid;
+    }
+    t->form = form;
+    return kOk;
+}
+
+int bhut_tree_accel_self(bhut_tree* t, double theta, double softening, double G, double* out)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (!t->built) { set_error("Tree must be built before evaluating accelerations"); return kNotBuilt; }
+    if (!out) { set_error("out is NULL"); return kInvalid; }
+    if (!(theta >= 0)) { set_error("theta must be non-negative, got %g", theta); return kInvalid; }
+    if (!(softening >= 0)) { set_error("softening must be non-negative, got %g", softening); return kInvalid; }
+    size_t bytes = sizeof(double) * t->n * t->dim;
+    OutTarget o;
+    BHUT_TRY(out_target(t, out, bytes, &o));
+    BHUT_TRY(traverse(t, t->sx.as<double>(), t->sy.as<double>(), t->sz.as<double>(),
+                      t->perm.as<int32_t>(), t->perm.as<int32_t>(), t->n, theta, softening, G,
+                      o.dev));
+    return finish_out(t, o, bytes, "accelerations");
+}
+
+int bhut_tree_accel_targets(bhut_tree* t, const double* targets, int64_t mt, double theta,
+                            double softening, double G, double* out)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (!t->built) { set_error("Tree must be built before evaluating accelerations"); return kNotBuilt; }
+    if (mt < 0 || (mt > 0 && (!targets || !out))) { set_error("invalid targets"); return kInvalid; }
+    if (!(theta >= 0)) { set_error("theta must be non-negative, got %g", theta); return kInvalid; }
+    if (!(softening >= 0)) { set_error("softening must be non-negative, got %g", softening); return kInvalid; }
+    if (mt == 0) return kOk;
+    if (mt > 0x7fffffffLL) { set_error("at most 2^31-1 targets are supported"); return kInvalid; }
+    cudaStream_t s = t->stream;
+    const int dim = t->dim;
+    size_t bytes = sizeof(double) * mt * dim;
+    BHUT_TRY(stage_in(t->tpos, targets, bytes, s));
+    // Morton-order the targets (their own box) so each warp's 32 targets are
+    // close together; results are scattered back to input order.
+    BHUT_TRY(sort_points(t, t->tpos.as<double>(), mt, t->tkeys, t->tperm, t->tbox));
+    for (DevBuf* b : {&t->tx, &t->ty, &t->tz}) BHUT_TRY(b->ensure(sizeof(double) * mt, s));
+    BHUT_TRY(launch_gather(t->tpos.as<double>(), nullptr, t->tperm.as<int32_t>(), mt, dim,
+                           t->tx.as<double>(), t->ty.as<double>(), t->tz.as<double>(), nullptr, s));
+    int st = check_err_word(t, "targets");
+    if (st != kOk) return st;
+    OutTarget o;
+    BHUT_TRY(out_target(t, out, bytes, &o));
+    BHUT_TRY(traverse(t, t->tx.as<double>(), t->ty.as<double>(), t->tz.as<double>(), nullptr,
+                      t->tperm.as<int32_t>(), mt, theta, softening, G, o.dev));
+    return finish_out(t, o, bytes, "accelerations at targets");
+}
+
+int bhut_tree_stats(const bhut_tree* t, int64_t* p2p, int64_t* m2p, int64_t* visits)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (p2p) *p2p = (int64_t)t->last_stats[0];
+    if (m2p) *m2p = (int64_t)t->last_stats[1];
+    if (visits) *visits = (int64_t)t->last_stats[2];
+    return kOk;
+}
+
+long long bhut_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int bhut_tree_info(const bhut_tree* t, int64_t* n, int64_t* num_nodes, int* dim, int* leaf_size)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (n) *n = t->built ? t->n : 0;
+    if (num_nodes) *num_nodes = t->built ? t->m : 0;
+    if (dim) *dim = t->dim;
+    if (leaf_size) *leaf_size = t->leaf;
+    return kOk;
+}
+
+int bhut_tree_export(const bhut_tree* t, double* center, double* half_size, double* mass,
+                     double* com, int64_t* first_child, int64_t* child_count, int64_t* start,
+                     int64_t* count, uint8_t* is_leaf, int64_t* perm)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (!t->built) { set_error("Tree not built. Call build() first."); return kNotBuilt; }
+    const int64_t m = t->m, n = t->n;
+    const int dim = t->dim;
+    cudaStream_t s = t->stream;
+    NodeCM* cm = new NodeCM[m];
+    int32_t* fc = new int32_t[m];
+    int32_t* st = new int32_t[m];
+    int32_t* ct = new int32_t[m];
+    int32_t* pm = new int32_t[n];
+    int rc = kOk;
+    cudaError_t e = cudaMemcpyAsync(cm, t->cm.p, sizeof(NodeCM) * m, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fc, t->first_child.p, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st, t->start.p, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ct, t->count.p, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pm, t->perm.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && center) e = cudaMemcpyAsync(center, t->center.p, sizeof(double) * m * dim, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && half_size) e = cudaMemcpyAsync(half_size, t->half.p, sizeof(double) * m, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        rc = cuda_status(e, "export");
+    } else {
+        for (int64_t k = 0; k < m; k++) {
+            if (mass) mass[k] = cm[k].w;
+            if (com) {
+                com[k * dim] = cm[k].x;
+                com[k * dim + 1] = cm[k].y;
+                if (dim == 3) com[k * dim + 2] = cm[k].z;
+            }
+            if (first_child) first_child[k] = fc[k];
+            if (child_count) child_count[k] = fc[k] < 0 ? 0 : 2;
+            if (start) start[k] = st[k];
+            if (count) count[k] = ct[k];
+            if (is_leaf) is_leaf[k] = fc[k] < 0 ? 1 : 0;
+        }
+        if (perm) for (int64_t i = 0; i < n; i++) perm[i] = pm[i];
+    }
+    delete[] cm; delete[] fc; delete[] st; delete[] ct; delete[] pm;
+    return rc;
+}
+
+void bhut_tree_destroy(bhut_tree* t)
+{
+    if (!t) return;
+    cudaStream_t s = t->stream;
+    DevBuf* all[] = {&t->pos, &t->mass, &t->keys, &t->perm, &t->sx, &t->sy, &t->sz, &t->sm,
+                     &t->cm, &t->size, &t->center, &t->half, &t->lo, &t->hi, &t->first_child,
+                     &t->start, &t->count, &t->parent, &t->leaf_list, &t->arrive,
+                     &t->sort_scratch, &t->box_partial, &t->box, &t->counters, &t->err, &t->stats,
+                     &t->tpos, &t->tkeys, &t->tperm, &t->tx, &t->ty, &t->tz, &t->tbox, &t->out};
+    for (DevBuf* b : all) b->release(s);
+    cudaStreamSynchronize(s);
+    if (t->own_stream) cudaStreamDestroy(s);
+    delete t;
+}
+
+int bhut_morton_keys(const double* positions, int64_t n, int dim, uint64_t* keys, void* stream)
+{
+    if (dim != 2 && dim != 3) { set_error("dim must be 2 or 3, got %d", dim); return kInvalid; }
+    if (n <= 0) { set_error("points array cannot be empty"); return kInvalid; }
+    bhut_tree* t = nullptr;
+    BHUT_TRY(bhut_tree_create(dim, 1, stream, &t));
+    int rc = stage_in(t->pos, positions, sizeof(double) * n * dim, t->stream);
+    if (rc == kOk) rc = t->box.ensure(sizeof(double) * 6, t->stream);
+    if (rc == kOk) rc = t->box_partial.ensure(sizeof(double) * 6 * 152 * 4, t->stream);
+    if (rc == kOk) rc = t->keys.ensure(sizeof(uint64_t) * n, t->stream);
+    if (rc == kOk) rc = launch_bbox(t->pos.as<double>(), n, dim, t->box_partial.as<double>(),
+                                    t->counters.as<unsigned>(), t->box.as<double>(),
+                                    t->err.as<unsigned>(), t->stream);
+    if (rc == kOk) rc = launch_morton(t->pos.as<double>(), n, dim, t->box.as<double>(),
+                                      t->keys.as<uint64_t>(), nullptr, t->stream);
+    if (rc == kOk) {
+        cudaError_t e = cudaMemcpyAsync(keys, t->keys.p, sizeof(uint64_t) * n, cudaMemcpyDefault,
+                                        t->stream);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy keys");
+    }
+    if (rc == kOk) rc = check_err_word(t, "morton keys");
+    bhut_tree_destroy(t);
+    return rc;
+}
+
+int bhut_morton_argsort(const double* positions, int64_t n, int dim, uint64_t* sorted_keys,
+                        int64_t* perm, void* stream)
+{
+    if (dim != 2 && dim != 3) { set_error("dim must be 2 or 3, got %d", dim); return kInvalid; }
+    if (n <= 0) { set_error("points array cannot be empty"); return kInvalid; }
+    bhut_tree* t = nullptr;
+    BHUT_TRY(bhut_tree_create(dim, 1, stream, &t));
+    int rc = stage_in(t->pos, positions, sizeof(double) * n * dim, t->stream);
+    if (rc == kOk) rc = sort_points(t, t->pos.as<double>(), n, t->keys, t->perm, t->box);
+    int32_t* p32 = nullptr;
+    if (rc == kOk && sorted_keys) {
+        cudaError_t e = cudaMemcpyAsync(sorted_keys, t->keys.p, sizeof(uint64_t) * n,
+                                        cudaMemcpyDefault, t->stream);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy keys");
+    }
+    if (rc == kOk && perm) {
+        p32 = new int32_t[n];
+        cudaError_t e = cudaMemcpyAsync(p32, t->perm.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                                        t->stream);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy perm");
+    }
+    if (rc == kOk) rc = check_err_word(t, "argsort");
+    if (rc == kOk && perm) {
+        if (is_device_pointer(perm)) {
+            int64_t* tmp = new int64_t[n];
+            for (int64_t i = 0; i < n; i++) tmp[i] = p32[i];
+            cudaError_t e = cudaMemcpy(perm, tmp, sizeof(int64_t) * n, cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) rc = cuda_status(e, "copy perm");
+            delete[] tmp;
+        } else {
+            for (int64_t i = 0; i < n; i++) perm[i] = p32[i];
+        }
+    }
+    delete[] p32;
+    bhut_tree_destroy(t);
+    return rc;
+}
+
+int bhut_direct_accelerations(const double* positions, const double* masses, int64_t n, int dim,
+                              const double* targets, int64_t mt, double softening, double G,
+                              double* out, void* stream)
+{
+    if (dim != 2 && dim != 3) { set_error("dim must be 2 or 3, got %d", dim); return kInvalid; }
+    if (n <= 0) { set_error("Cannot build tree with zero particles"); return kInvalid; }
+    if (!targets && mt != n) { set_error("self accelerations need m == n"); return kInvalid; }
+    if (mt <= 0) return kOk;
+    bhut_tree* t = nullptr;
+    BHUT_TRY(bhut_tree_create(dim, 1, stream, &t));
+    cudaStream_t s = t->stream;
+    int rc = stage_in(t->pos, positions, sizeof(double) * n * dim, s);
+    if (rc == kOk) rc = stage_in(t->mass, masses, sizeof(double) * n, s);
+    if (rc == kOk && targets) rc = stage_in(t->tpos, targets, sizeof(double) * mt * dim, s);
+    DevBuf self_idx;
+    if (rc == kOk && !targets) {
+        rc = self_idx.ensure(sizeof(int64_t) * n, s);
+        if (rc == kOk) {
+            int64_t* h = new int64_t[n];
+            for (int64_t i = 0; i < n; i++) h[i] = i;
+            cudaError_t e = cudaMemcpyAsync(self_idx.p, h, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) rc = cuda_status(e, "copy index");
+            delete[] h;
+        }
+    }
+    OutTarget o{nullptr, nullptr};
+    size_t bytes = sizeof(double) * mt * dim;
+    if (rc == kOk) rc = out_target(t, out, bytes, &o);
+    if (rc == kOk) rc = launch_direct(t->pos.as<double>(), t->mass.as<double>(), n, dim,
+                                      targets ? t->tpos.as<double>() : nullptr,
+                                      targets ? nullptr : self_idx.as<int64_t>(), mt, softening, G,
+                                      o.dev, s);
+    if (rc == kOk) rc = finish_out(t, o, bytes, "direct sum");
+    self_idx.release(s);
+    bhut_tree_destroy(t);
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,77 @@
+// Shared definitions for the GB300 Barnes-Hut engine (sm_103a).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bhut {
+
+// Status codes returned through the C ABI (include/bhut_gb300.h).
+enum Status : int {
+    kOk = 0,
+    kInvalid = 1,        // bad argument (maps to ValueError)
+    kNotBuilt = 2,       // tree not built
+    kCuda = 3,           // CUDA runtime error
+    kNoMemory = 4,       // device allocation failed
+    kDeviceFlag = 5,     // a kernel raised its error word (stack overflow, ...)
+    kInternal = 6,
+};
+
+// Error word bits written by kernels (never a trap).
+enum DeviceError : unsigned {
+    kErrStackOverflow = 1u,
+    kErrNonFinite = 2u,
+    kErrBadNode = 4u,
+    kErrScratchSize = 8u,
+};
+
+constexpr int kWarp = 32;
+constexpr int kStackDepth = 64;     // per-warp traversal stack entries
+
+void set_error(const char* fmt, ...);
+// Counts kernel launches made by the library (reported by bhut_launch_count).
+void note_launches(long long k);
+int cuda_status(cudaError_t e, const char* what);
+
+#define BHUT_CUDA(call)                                              \
+    do {                                                             \
+        cudaError_t e__ = (call);                                    \
+        if (e__ != cudaSuccess) return ::bhut::cuda_status(e__, #call); \
+    } while (0)
+
+#define BHUT_TRY(call)                     \
+    do {                                   \
+        int s__ = (call);                  \
+        if (s__ != ::bhut::kOk) return s__; \
+    } while (0)
+
+inline unsigned grid_for(int64_t n, int block, unsigned cap = 152u * 16u)
+{
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned)g;
+}
+
+// ---------------------------------------------------------------------------
+// Radix sort of (uint64 key, int32 value) pairs, stable, LSD, 8-bit digits.
+// ---------------------------------------------------------------------------
+struct SortScratch {
+    uint64_t* keys_alt = nullptr;
+    int32_t* vals_alt = nullptr;
+    uint32_t* tile_counts = nullptr;   // 256 * tiles
+    uint32_t* block_sums = nullptr;    // scan partials
+    int64_t capacity = 0;
+    int64_t tile_capacity = 0;
+};
+constexpr int kSortTile = 4096;        // keys per tile (8 warps x 512)
+constexpr int kSortThreads = 256;
+
+int64_t sort_tiles(int64_t n);
+size_t sort_scratch_bytes(int64_t n);
+// Sorts keys[0..n) ascending with values carried along.  `bits` is the
+// number of low key bits that can be non-zero (passes = ceil(bits / 8)).
+// The result ends in keys/vals.  Scratch must hold sort_scratch_bytes(n).
+int radix_sort_pairs(uint64_t* keys, int32_t* vals, int64_t n, int bits, void* scratch,
+                     cudaStream_t stream);
+
+}  // namespace bhut

@@ -1,0 +1,84 @@
+// Device-side tree layout shared by the build, refit and traversal kernels.
+#pragma once
+#include "common.cuh"
+
+namespace bhut {
+
+// Centre of mass and mass of a node, one 32-byte load.
+struct __align__(32) NodeCM {
+    double x, y, z, w;
+};
+
+// Node arrays are indexed by the reference's node id (bhut/tree/build.py:
+// the k-th internal node in pop order of the build stack has children 2k+1
+// and 2k+2).  Particles are held as Morton-sorted SoA.
+struct TreeDev {
+    int dim;
+    int leaf_size;
+    int64_t n;              // particles
+    int64_t m;              // nodes
+    // Morton-sorted particles (SoA) and their original indices
+    const double* sx;
+    const double* sy;
+    const double* sz;
+    const double* sm;
+    const int32_t* perm;
+    // nodes
+    const NodeCM* cm;      // (com.x, com.y, com.z, mass)
+    const double* size;     // 2 * half_size (the opening-test node size)
+    const int32_t* first_child;  // -1 for a leaf
+    const int32_t* start;
+    const int32_t* count;
+};
+
+// Geometry of the count-split topology for (n, leaf_size).  The counts at
+// depth d are floor(n / 2^d) or that plus one, so per depth only two count
+// values and two subtree internal-node counts exist.
+constexpr int kMaxDepth = 64;
+struct TopoTables {
+    int depth;                     // deepest level (all nodes there are leaves)
+    int64_t n;
+    int leaf_size;
+    int64_t cnt_lo[kMaxDepth];     // floor(n / 2^d)
+    int64_t internal[kMaxDepth][2];  // internal-node count of a subtree with cnt_lo[d] + {0,1}
+    int64_t num_nodes;
+    int64_t num_leaves;
+    int64_t slots;                 // 2^(depth+1) - 1 BFS slots
+};
+
+int make_topo_tables(int64_t n, int leaf_size, TopoTables* t);
+
+// Node arrays written by the bottom-up pass.
+struct NodeOut {
+    NodeCM* cm;        // (com, mass)
+    double* size;       // 2 * half_size
+    double* center;     // dim per node
+    double* half;
+    double* lo;         // 3 per node (AABB scratch)
+    double* hi;
+};
+
+// Kernel launchers (build.cu, traverse.cu).
+int launch_bbox(const double* pos, int64_t n, int dim, double* partial, unsigned* counter,
+                double* box, unsigned* err, cudaStream_t s);
+int launch_morton(const double* pos, int64_t n, int dim, const double* box, uint64_t* keys,
+                  int32_t* idx, cudaStream_t s);
+int launch_gather(const double* pos, const double* mass, const int32_t* perm, int64_t n, int dim,
+                  double* sx, double* sy, double* sz, double* sm, cudaStream_t s);
+int launch_topology(const TopoTables& tt, int32_t* first_child, int32_t* start, int32_t* count,
+                    int32_t* parent, int32_t* leaf_list, unsigned* leaf_counter, cudaStream_t s);
+int launch_bottom_up(const TreeDev& t, const int32_t* leaf_list, int64_t num_leaves,
+                     const int32_t* first_child, const int32_t* start, const int32_t* count,
+                     const int32_t* parent, unsigned* arrive, NodeOut o, bool refit,
+                     const double* opos, const double* omass, cudaStream_t s);
+int launch_outside_root(const double* pos, int64_t n, int dim, const double* center0,
+                        const double* half0, unsigned* flag, cudaStream_t s);
+int launch_traverse_exact(const TreeDev& t, const double* tx, const double* ty, const double* tz,
+                          const int32_t* self_id, const int32_t* out_idx, int64_t nt, double theta,
+                          double eps, double G, double* out, unsigned* err,
+                          unsigned long long* stats, cudaStream_t s);
+int launch_direct(const double* pos, const double* mass, int64_t n, int dim, const double* targets,
+                  const int64_t* self_id, int64_t nt, double eps, double G, double* out,
+                  cudaStream_t s);
+
+}  // namespace bhut

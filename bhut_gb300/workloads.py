@@ -1,0 +1,75 @@
+"""Seeded synthetic N-body systems used by the tests and the benchmark.
+
+There is no public dataset for this engine; every workload is generated from
+a seed with numpy's PCG64 ``default_rng``:
+
+* ``gaussian``: i.i.d. standard-normal positions, unit masses (the
+  CPU-runnable 10,000-particle case).
+* ``plummer``: Plummer sphere, r = a / sqrt(u^(-2/3) - 1) with radii beyond
+  ``rmax * a`` redrawn, isotropic directions, equal masses 1/N.
+* ``uniform_cube``: uniform in a centred cube of the given side.
+* ``galaxy``: 70 % exponential disc (radial scale ``rd`` drawn from
+  Gamma(2, rd), sech^2 vertical profile z = z0 * atanh(2u - 1)) and 30 %
+  Hernquist bulge (r = a sqrt(u) / (1 - sqrt(u))), equal masses 1/N.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _isotropic(rng: np.random.Generator, n: int) -> np.ndarray:
+    cos_t = rng.uniform(-1.0, 1.0, n)
+    phi = rng.uniform(0.0, 2.0 * np.pi, n)
+    sin_t = np.sqrt(np.maximum(0.0, 1.0 - cos_t * cos_t))
+    return np.stack([sin_t * np.cos(phi), sin_t * np.sin(phi), cos_t], axis=1)
+
+
+def gaussian(n: int, seed: int = 0, dim: int = 3):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal((n, dim)), np.ones(n)
+
+
+def plummer(n: int, seed: int = 0, a: float = 1.0, rmax: float = 20.0):
+    rng = np.random.default_rng(seed)
+    r = np.empty(n)
+    todo = np.arange(n)
+    while len(todo):
+        u = rng.uniform(0.0, 1.0, len(todo))
+        u = np.where(u <= 0.0, np.finfo(float).tiny, u)
+        rr = a / np.sqrt(u ** (-2.0 / 3.0) - 1.0)
+        ok = rr <= rmax * a
+        r[todo[ok]] = rr[ok]
+        todo = todo[~ok]
+    pos = _isotropic(rng, n) * r[:, None]
+    return pos, np.full(n, 1.0 / n)
+
+
+def uniform_cube(n: int, seed: int = 0, side: float = 10.0, dim: int = 3):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-side / 2, side / 2, (n, dim)), np.full(n, 1.0 / max(n, 1))
+
+
+def galaxy(n: int, seed: int = 0, rd: float = 3.0, z0: float = 0.3, a_bulge: float = 0.5,
+           disc_fraction: float = 0.7):
+    rng = np.random.default_rng(seed)
+    nd = int(round(disc_fraction * n))
+    nb = n - nd
+    R = rng.gamma(2.0, rd, nd)
+    phi = rng.uniform(0.0, 2.0 * np.pi, nd)
+    u = rng.uniform(0.0, 1.0, nd)
+    u = np.clip(u, 1e-15, 1.0 - 1e-15)
+    z = z0 * np.arctanh(2.0 * u - 1.0)
+    disc = np.stack([R * np.cos(phi), R * np.sin(phi), z], axis=1)
+    ub = rng.uniform(0.0, 1.0, nb)
+    ub = np.clip(ub, 0.0, 1.0 - 1e-12)
+    s = np.sqrt(ub)
+    rb = a_bulge * s / (1.0 - s)
+    bulge = _isotropic(rng, nb) * rb[:, None]
+    pos = np.concatenate([disc, bulge], axis=0)
+    return pos, np.full(n, 1.0 / n)
+
+
+def cube_targets(m: int, seed: int = 0, side: float = 10.0, dim: int = 3) -> np.ndarray:
+    """External targets uniform in a centred cube of the given side."""
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-side / 2, side / 2, (m, dim))

@@ -1,0 +1,133 @@
+/*
+ * bhut_gb300.h -- C ABI of the GB300 Barnes-Hut engine (libbhut_gb300.so).
+ *
+ * A drop-in for the compute behind bhut 0.1.0's public API
+ * (bhut/api.py: accelerations, Tree.build/refit/rebuild/accelerations).
+ * Plain pointers and sizes only.  Every array pointer may be host memory or
+ * device memory of the current CUDA device (detected per call); arrays are
+ * C-ordered float64 (positions (n, dim), masses (n,), accelerations
+ * (n, dim)).  Calls are synchronous: outputs are complete on return.
+ * Every call returns a status code (BHUT_OK == 0); bhut_last_error() gives the
+ * message of the last failure on the calling thread.  Kernels never trap: a
+ * device-side problem sets an error word that the call turns into
+ * BHUT_EDEVICE.
+ *
+ * Handles are not thread-safe for concurrent mutation (as the reference's
+ * Tree); concurrent calls on different handles are fine.
+ */
+#ifndef BHUT_GB300_H
+#define BHUT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define BHUT_API __attribute__((visibility("default")))
+#else
+#define BHUT_API
+#endif
+
+#define BHUT_OK 0
+#define BHUT_EINVAL 1      /* invalid argument (ValueError in the reference) */
+#define BHUT_ENOTBUILT 2   /* tree not built */
+#define BHUT_ECUDA 3       /* CUDA runtime failure */
+#define BHUT_ENOMEM 4      /* device allocation failed */
+#define BHUT_EDEVICE 5     /* a kernel reported an error (e.g. stack overflow) */
+#define BHUT_EINTERNAL 6
+
+/* Traversal arithmetic (bhut_tree_set_form). */
+#define BHUT_FORM_EXACT 0  /* FP64; pair terms bit-identical to the reference's Numba loop */
+#define BHUT_FORM_FAST 1   /* FP64-accurate float-float on the FP32 pipe (default) */
+#define BHUT_FORM_FP32 2   /* precision form: FP32 with Kahan-compensated sums */
+
+typedef struct bhut_tree bhut_tree;
+
+/* Library version string. */
+BHUT_API const char *bhut_version(void);
+
+/* Copies the last error message of this thread into buf (NUL-terminated);
+ * returns its full length. */
+BHUT_API int bhut_last_error(char *buf, size_t len);
+
+/* New, unbuilt tree handle.  Replaces Tree.__init__ (bhut/api.py:470-495)
+ * minus the array validation that the host layer does.  stream: a
+ * cudaStream_t, or NULL for a stream owned by the handle. */
+BHUT_API int bhut_tree_create(int dim, int leaf_size, void *stream, bhut_tree **out);
+
+/* Builds the tree over n particles.  Replaces build_tree
+ * (bhut/api.py:155-191 -> bhut/tree/build.py:19-107): bounding box, Morton
+ * keys, stable sort, count-split topology, node AABBs, masses, COMs.
+ * BHUT_EINVAL for n == 0 ("Cannot build tree with zero particles") or
+ * non-finite positions. */
+BHUT_API int bhut_tree_build(bhut_tree *t, const double *positions, const double *masses, int64_t n);
+
+/* Tree.refit (bhut/api.py:513-562): when any particle lies outside 1.1x the
+ * root box (bhut/tree/refit.py:195-251) or n differs, rebuilds and sets
+ * *rebuilt = 1; else refit_tree (bhut/tree/refit.py:17-109) with stale node
+ * geometry and permutation.  masses == NULL keeps the stored masses. */
+BHUT_API int bhut_tree_refit(bhut_tree *t, const double *positions, const double *masses, int64_t n,
+                    int *rebuilt);
+
+/* Tree.rebuild (bhut/api.py:564-606).  masses == NULL keeps the stored
+ * masses (n must then equal the stored n). */
+BHUT_API int bhut_tree_rebuild(bhut_tree *t, const double *positions, const double *masses, int64_t n);
+
+/* Self accelerations of the stored particles, out (n, dim).  Replaces
+ * barnes_hut_accelerations (bhut/traverse/bh.py:428-548). */
+BHUT_API int bhut_tree_accel_self(bhut_tree *t, double theta, double softening, double G, double *out);
+
+/* Accelerations at m external targets (m, dim), out (m, dim).  Replaces
+ * barnes_hut_accelerations_targets (bhut/traverse/bh.py:30-146). */
+BHUT_API int bhut_tree_accel_targets(bhut_tree *t, const double *targets, int64_t m, double theta,
+                            double softening, double G, double *out);
+
+/* Selects the traversal arithmetic (BHUT_FORM_*). */
+BHUT_API int bhut_tree_set_form(bhut_tree *t, int form);
+
+/* Interaction counts of the last traversal on this handle: pair (P2P)
+ * evaluations, monopole (M2P) evaluations and node visits, summed over
+ * targets.  The device-side counterpart of compute_tree_statistics
+ * (bhut/traverse/bh.py:604-700), counting pairs actually evaluated (the
+ * target itself and zero-distance pairs are not counted). */
+BHUT_API int bhut_tree_stats(const bhut_tree *t, int64_t *p2p, int64_t *m2p, int64_t *visits);
+
+/* Total number of kernels this library has launched in the process. */
+BHUT_API long long bhut_launch_count(void);
+
+/* n, node count, dim, leaf size of a built tree. */
+BHUT_API int bhut_tree_info(const bhut_tree *t, int64_t *n, int64_t *num_nodes, int *dim, int *leaf_size);
+
+/* Copies the TreeData arrays (bhut/tree/node.py:15-77) to host buffers sized
+ * for num_nodes (center and com: num_nodes x dim) and n (perm).  Any pointer
+ * may be NULL to skip that array. */
+BHUT_API int bhut_tree_export(const bhut_tree *t, double *center, double *half_size, double *mass,
+                     double *com, int64_t *first_child, int64_t *child_count, int64_t *start,
+                     int64_t *count, uint8_t *is_leaf, int64_t *perm);
+
+/* Releases the handle and its device memory. */
+BHUT_API void bhut_tree_destroy(bhut_tree *t);
+
+/* Morton keys in input order: aabb + normalize_to_unit + morton_codes
+ * (bhut/space/bbox.py:14-96, bhut/utils/morton.py:48-102). */
+BHUT_API int bhut_morton_keys(const double *positions, int64_t n, int dim, uint64_t *keys, void *stream);
+
+/* sort_by_morton (bhut/utils/morton.py:105-147): sorted keys and the stable
+ * permutation (np.argsort(kind='stable')). */
+BHUT_API int bhut_morton_argsort(const double *positions, int64_t n, int dim, uint64_t *sorted_keys,
+                        int64_t *perm, void *stream);
+
+/* FP64 direct sum (the theta = 0 limit) at m targets, or self accelerations
+ * when targets == NULL (then m must equal n). */
+BHUT_API int bhut_direct_accelerations(const double *positions, const double *masses, int64_t n, int dim,
+                              const double *targets, int64_t m, double softening, double G,
+                              double *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BHUT_GB300_H */

@@ -1,0 +1,186 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the reference's
+golden outputs and the oracle.
+
+Bars (the engine's contract):
+  * Morton keys, permutation, topology, node AABBs (center, half_size),
+    masses and centres of mass: bit-exact.
+  * accelerations, form "exact": <= 1e-12 relative L2 against the reference
+    fixtures and the oracle.
+  * accelerations, every form that claims FP64 accuracy: <= 1e-10 relative L2
+    at N=1,000,000 Plummer, theta=0.5 (the plain-path bar).
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import bhut_gb300 as bh
+from bhut_gb300 import workloads
+from conftest import TREE_FIELDS, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+EXACT_RTOL = 1e-12
+PLAIN_RTOL = 1e-10
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _engine(engine_lib):
+    yield
+
+
+def _tree_arrays_equal(td, g, prefix):
+    for f in TREE_FIELDS:
+        a = np.asarray(getattr(td, f))
+        b = g[prefix + f]
+        assert a.shape == b.shape, (prefix, f, a.shape, b.shape)
+        assert np.array_equal(a.astype(b.dtype), b), f"{prefix}{f} differs"
+
+
+def test_morton_keys_and_stable_perm(golden_small, golden_gauss):
+    g = golden_small
+    for name in g["names"]:
+        pos, keys = g[f"{name}__pos"], g[f"{name}__keys"]
+        assert np.array_equal(bh.morton_keys(pos), keys), name
+        sk, perm = bh.morton_argsort(pos)
+        ref_perm = np.argsort(keys, kind="stable")
+        assert np.array_equal(perm, ref_perm), name
+        assert np.array_equal(sk, keys[ref_perm]), name
+    gg = golden_gauss
+    assert np.array_equal(bh.morton_keys(gg["pos"]), gg["keys"])
+    sk, perm = bh.morton_argsort(gg["pos"])
+    assert np.array_equal(perm, gg["tree_perm"])
+
+
+def test_radix_sort_ties_and_sizes(oracle_mod):
+    """Stable order with many equal keys, at sizes around the sort tile."""
+    rng = np.random.default_rng(3)
+    for n in (1, 2, 31, 4095, 4096, 4097, 100_003):
+        pos = rng.integers(0, 4, (n, 3)).astype(np.float64)   # heavy key ties
+        keys, perm = bh.morton_argsort(pos)
+        ref = oracle_mod.morton_codes(pos)
+        assert np.array_equal(perm, np.argsort(ref, kind="stable")), n
+        assert np.array_equal(keys, np.sort(ref, kind="stable")), n
+
+
+def test_small_systems_trees(golden_small):
+    g = golden_small
+    for name in g["names"]:
+        pos, m = g[f"{name}__pos"], g[f"{name}__masses"]
+        for L in (1, 4, 32):
+            td = bh.build_tree(pos, m, leaf_size=L, backend="auto", dim=pos.shape[1])
+            _tree_arrays_equal(td, g, f"{name}__L{L}__")
+
+
+@pytest.mark.parametrize("form", ["exact"])
+def test_small_systems_forces(golden_small, oracle_mod, form):
+    g = golden_small
+    for name in g["names"]:
+        pos, m = g[f"{name}__pos"], g[f"{name}__masses"]
+        tg = g[f"{name}__targets"]
+        dim = pos.shape[1]
+        for L in (1, 4, 32):
+            tree = bh.Tree(pos, m, leaf_size=L, dim=dim, form=form).build()
+            for theta in (0.0, 0.7):
+                for eps in (0.0, 0.01):
+                    tag = f"{name}__L{L}__t{theta}__e{eps}"
+                    got = tree.accelerations(theta=theta, softening=eps)
+                    assert rel_l2(got, g[tag + "__self"]) <= EXACT_RTOL, tag
+                    got = tree.accelerations(tg, theta=theta, softening=eps)
+                    assert rel_l2(got, g[tag + "__ext"]) <= EXACT_RTOL, tag
+            tree.close()
+
+
+def test_gauss10k_full(golden_gauss, oracle_mod):
+    g = golden_gauss
+    pos, m = g["pos"], g["masses"]
+    L, eps = int(g["leaf_size"]), float(g["softening"])
+    tree = bh.Tree(pos, m, leaf_size=L).build()
+    _tree_arrays_equal(tree._tree, g, "tree_")
+    acc = tree.accelerations(theta=0.5, softening=eps)
+    assert acc.dtype == np.float64 and acc.shape == pos.shape
+    assert rel_l2(acc[g["sample"]], g["acc_theta05"]) <= EXACT_RTOL
+    # every target against the oracle (scalar FP64 restatement, same pair math)
+    ot = oracle_mod.build_tree(pos, m, L)
+    ref = oracle_mod.accelerations(ot, pos, m, theta=0.5, softening=eps)
+    assert rel_l2(acc, ref) <= 1e-14
+    acc0 = tree.accelerations(theta=0.0, softening=eps)
+    assert rel_l2(acc0[g["sample0"]], g["acc_theta0"]) <= EXACT_RTOL
+    at = tree.accelerations(g["targets"], theta=0.5, softening=eps)
+    assert rel_l2(at, g["acc_targets_theta05"]) <= EXACT_RTOL
+    tree.close()
+
+
+def test_refit_and_fallback(golden_refit, oracle_mod):
+    g = golden_refit
+    for tag in ("plain", "negmass"):
+        pos, m = g[f"{tag}__pos"], g[f"{tag}__masses"]
+        pos2, m2 = g[f"{tag}__pos2"], g[f"{tag}__masses2"]
+        tree = bh.Tree(pos, m, leaf_size=16).build()
+        tree.refit(pos2, m2)
+        _tree_arrays_equal(tree._tree, g, f"{tag}__refit__")
+        got = tree.accelerations(theta=0.5, softening=0.01)
+        assert rel_l2(got[g[f"{tag}__sample"]], g[f"{tag}__acc"]) <= EXACT_RTOL
+        tree.close()
+    tree = bh.Tree(g["moved__pos"], g["moved__masses"], leaf_size=8).build()
+    tree.refit(g["moved__pos3"])
+    _tree_arrays_equal(tree._tree, g, "moved__tree__")
+    tree.close()
+
+
+def test_direct_sum_matches_oracle(oracle_mod):
+    pos, m = workloads.plummer(3000, seed=9)
+    got = bh.direct_accelerations(pos, m, softening=0.01)
+    ref = oracle_mod.direct_sum(pos, m, softening=0.01)
+    assert rel_l2(got, ref) <= 1e-14
+    tg = workloads.cube_targets(500, seed=2, side=4.0)
+    got = bh.direct_accelerations(pos, m, softening=0.01, targets=tg)
+    ref = oracle_mod.direct_sum(pos, m, softening=0.01, targets=tg)
+    assert rel_l2(got, ref) <= 1e-14
+
+
+def _digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.fixture(scope="module")
+def plummer_1m(golden_plummer):
+    g = golden_plummer
+    pos, m = workloads.plummer(int(g["n"]), seed=int(g["seed"]))
+    return pos, m
+
+
+def test_plummer_1m_tree_digests(golden_plummer, plummer_1m):
+    g = golden_plummer
+    dig = dict(zip(g["digest_names"], g["digest_values"]))
+    pos, m = plummer_1m
+    assert _digest(pos) == dig["pos"]
+    assert _digest(bh.morton_keys(pos)) == dig["keys"]
+    td = bh.build_tree(pos, m, leaf_size=int(g["leaf_size"]), backend="auto", dim=3)
+    for f in TREE_FIELDS:
+        a = np.asarray(getattr(td, f))
+        a = a.astype(np.int64) if a.dtype.kind == "i" else a
+        assert _digest(a) == dig[f], f
+
+
+@pytest.mark.parametrize("form", ["exact"])
+def test_plummer_1m_forces(golden_plummer, plummer_1m, oracle_mod, form):
+    """The plain-path bar: <= 1e-10 relative L2 at N=1M Plummer, theta=0.5,
+    on the reference's own sample and on 4096 oracle-checked targets."""
+    g = golden_plummer
+    pos, m = plummer_1m
+    eps = float(g["softening"])
+    tree = bh.Tree(pos, m, leaf_size=32, form=form).build()
+    acc = tree.accelerations(theta=0.5, softening=eps)
+    assert rel_l2(acc[g["sample"]], g["acc_theta05"]) <= PLAIN_RTOL
+    idx = np.random.default_rng(17).choice(len(pos), 4096, replace=False)
+    ot = oracle_mod.build_tree(pos, m, 32)
+    ref = oracle_mod.accelerations(ot, pos, m, theta=0.5, softening=eps, self_index=idx)
+    assert rel_l2(acc[idx], ref) <= PLAIN_RTOL
+    # 250,000 external targets uniform in a centred cube of side 10
+    tg = workloads.cube_targets(250_000, seed=4, side=10.0)
+    at = tree.accelerations(tg, theta=0.5, softening=eps)
+    sub = idx[:2048] % len(tg)
+    ref_t = oracle_mod.accelerations(ot, pos, m, theta=0.5, softening=eps, targets=tg[sub])
+    assert rel_l2(at[sub], ref_t) <= PLAIN_RTOL
+    tree.close()
