@@ -179,7 +179,7 @@ __global__ void k_gather_sorted(const double* __restrict__ pos, const double* __
 __global__ void k_topology(TopoTables tt, int32_t* __restrict__ first_child,
                            int32_t* __restrict__ start, int32_t* __restrict__ count,
                            int32_t* __restrict__ parent, int32_t* __restrict__ leaf_list,
-                           unsigned* __restrict__ leaf_counter)
+                           unsigned* __restrict__ leaf_counter, unsigned* __restrict__ err)
 {
     const int64_t L = tt.leaf_size;
     for (int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; slot < tt.slots;
@@ -208,13 +208,15 @@ __global__ void k_topology(TopoTables tt, int32_t* __restrict__ first_child,
             }
         }
         if (!exists) continue;
+        if (id >= tt.num_nodes || s + c > tt.n) { atomicOr(err, kErrBadNode); continue; }
         start[id] = (int32_t)s;
         count[id] = (int32_t)c;
         parent[id] = (int32_t)par;
         if (c <= L) {
             first_child[id] = -1;
             unsigned li = atomicAdd(leaf_counter, 1u);
-            leaf_list[li] = (int32_t)id;
+            if (li < tt.num_leaves) leaf_list[li] = (int32_t)id;
+            else atomicOr(err, kErrBadNode);
         } else {
             first_child[id] = (int32_t)(2 * k + 1);
         }
@@ -395,17 +397,26 @@ __global__ void k_bottom_up(TreeDev t, const int32_t* __restrict__ leaf_list, in
                             const int32_t* __restrict__ start, const int32_t* __restrict__ count,
                             const int32_t* __restrict__ parent, unsigned* __restrict__ arrive,
                             NodeOut o, bool refit, const double* __restrict__ opos,
-                            const double* __restrict__ omass)
+                            const double* __restrict__ omass, unsigned* __restrict__ err)
 {
     for (int64_t li = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; li < num_leaves;
          li += (int64_t)gridDim.x * blockDim.x) {
         int32_t id = leaf_list[li];
+        if (id < 0 || id >= t.m || start[id] < 0 || count[id] < 1 ||
+            (int64_t)start[id] + count[id] > t.n) {
+            atomicOr(err, kErrBadNode);
+            continue;
+        }
         leaf_node(id, t.dim, refit, t, opos, omass, start, count, o);
         // climb: each step is taken by the second child to arrive
         int32_t node = id;
         while (true) {
             int32_t p = parent[node];
             if (p < 0) break;
+            if (p >= t.m || first_child[p] < 1 || first_child[p] + 1 >= t.m) {
+                atomicOr(err, kErrBadNode);
+                break;
+            }
             __threadfence();
             unsigned prev = atomicAdd(&arrive[p], 1u);
             if (prev == 0) break;
@@ -500,11 +511,12 @@ int launch_gather(const double* pos, const double* mass, const int32_t* perm, in
 }
 
 int launch_topology(const TopoTables& tt, int32_t* first_child, int32_t* start, int32_t* count,
-                    int32_t* parent, int32_t* leaf_list, unsigned* leaf_counter, cudaStream_t s)
+                    int32_t* parent, int32_t* leaf_list, unsigned* leaf_counter, unsigned* err,
+                    cudaStream_t s)
 {
     BHUT_CUDA(cudaMemsetAsync(leaf_counter, 0, sizeof(unsigned), s));
     k_topology<<<grid_for(tt.slots, 256), 256, 0, s>>>(tt, first_child, start, count, parent,
-                                                       leaf_list, leaf_counter);
+                                                       leaf_list, leaf_counter, err);
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
     return kOk;
@@ -513,12 +525,12 @@ int launch_topology(const TopoTables& tt, int32_t* first_child, int32_t* start, 
 int launch_bottom_up(const TreeDev& t, const int32_t* leaf_list, int64_t num_leaves,
                      const int32_t* first_child, const int32_t* start, const int32_t* count,
                      const int32_t* parent, unsigned* arrive, NodeOut o, bool refit,
-                     const double* opos, const double* omass, cudaStream_t s)
+                     const double* opos, const double* omass, unsigned* err, cudaStream_t s)
 {
     BHUT_CUDA(cudaMemsetAsync(arrive, 0, sizeof(unsigned) * (size_t)t.m, s));
     k_bottom_up<<<grid_for(num_leaves, 128), 128, 0, s>>>(t, leaf_list, num_leaves, first_child,
                                                           start, count, parent, arrive, o, refit,
-                                                          opos, omass);
+                                                          opos, omass, err);
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
     return kOk;

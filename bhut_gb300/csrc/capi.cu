@@ -203,13 +203,15 @@ int do_build(bhut_tree* t, int64_t n)
         BHUT_TRY(t->leaf_list.ensure(sizeof(int32_t) * t->tt.num_leaves, s));
         BHUT_TRY(launch_topology(t->tt, t->first_child.as<int32_t>(), t->start.as<int32_t>(),
                                  t->count.as<int32_t>(), t->parent.as<int32_t>(),
-                                 t->leaf_list.as<int32_t>(), t->counters.as<unsigned>() + 1, s));
+                                 t->leaf_list.as<int32_t>(), t->counters.as<unsigned>() + 1,
+                                 t->err.as<unsigned>(), s));
         t->topo_valid = true;
     }
     BHUT_TRY(launch_bottom_up(t->dev(), t->leaf_list.as<int32_t>(), t->tt.num_leaves,
                               t->first_child.as<int32_t>(), t->start.as<int32_t>(),
                               t->count.as<int32_t>(), t->parent.as<int32_t>(),
-                              t->arrive.as<unsigned>(), t->nodes(), false, nullptr, nullptr, s));
+                              t->arrive.as<unsigned>(), t->nodes(), false, nullptr, nullptr,
+                              t->err.as<unsigned>(), s));
     int st = check_err_word(t, "build");
     if (st != kOk) {
         t->built = false;
@@ -382,7 +384,7 @@ int bhut_tree_refit(bhut_tree* t, const double* positions, const double* masses,
                               t->first_child.as<int32_t>(), t->start.as<int32_t>(),
                               t->count.as<int32_t>(), t->parent.as<int32_t>(),
                               t->arrive.as<unsigned>(), t->nodes(), true, t->pos.as<double>(),
-                              t->mass.as<double>(), s));
+                              t->mass.as<double>(), t->err.as<unsigned>(), s));
     return check_err_word(t, "refit");
 }
 

@@ -66,11 +66,12 @@ int launch_morton(const double* pos, int64_t n, int dim, const double* box, uint
 int launch_gather(const double* pos, const double* mass, const int32_t* perm, int64_t n, int dim,
                   double* sx, double* sy, double* sz, double* sm, cudaStream_t s);
 int launch_topology(const TopoTables& tt, int32_t* first_child, int32_t* start, int32_t* count,
-                    int32_t* parent, int32_t* leaf_list, unsigned* leaf_counter, cudaStream_t s);
+                    int32_t* parent, int32_t* leaf_list, unsigned* leaf_counter, unsigned* err,
+                    cudaStream_t s);
 int launch_bottom_up(const TreeDev& t, const int32_t* leaf_list, int64_t num_leaves,
                      const int32_t* first_child, const int32_t* start, const int32_t* count,
                      const int32_t* parent, unsigned* arrive, NodeOut o, bool refit,
-                     const double* opos, const double* omass, cudaStream_t s);
+                     const double* opos, const double* omass, unsigned* err, cudaStream_t s);
 int launch_outside_root(const double* pos, int64_t n, int dim, const double* center0,
                         const double* half0, unsigned* flag, cudaStream_t s);
 int launch_traverse_exact(const TreeDev& t, const double* tx, const double* ty, const double* tz,

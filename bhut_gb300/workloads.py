@@ -7,6 +7,10 @@ a seed with numpy's PCG64 ``default_rng``:
   CPU-runnable 10,000-particle case).
 * ``plummer``: Plummer sphere, r = a / sqrt(u^(-2/3) - 1) with radii beyond
   ``rmax * a`` redrawn, isotropic directions, equal masses 1/N.
+  u^(1/3) is drawn as the largest of three uniforms (its CDF is v^3), so
+  r = a v / sqrt(1 - v^2), and directions use Marsaglia's disc method: only
+  correctly rounded IEEE operations are involved, so the same seed gives
+  bit-identical systems on x86-64 and aarch64.
 * ``uniform_cube``: uniform in a centred cube of the given side.
 * ``galaxy``: 70 % exponential disc (radial scale ``rd`` drawn from
   Gamma(2, rd), sech^2 vertical profile z = z0 * atanh(2u - 1)) and 30 %
@@ -29,18 +33,39 @@ def gaussian(n: int, seed: int = 0, dim: int = 3):
     return rng.standard_normal((n, dim)), np.ones(n)
 
 
+def _marsaglia_directions(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Isotropic unit vectors from points uniform in the unit disc."""
+    out = np.empty((n, 3))
+    todo = np.arange(n)
+    while len(todo):
+        x1 = rng.uniform(-1.0, 1.0, len(todo))
+        x2 = rng.uniform(-1.0, 1.0, len(todo))
+        s = x1 * x1 + x2 * x2
+        ok = (s < 1.0) & (s > 0.0)
+        idx = todo[ok]
+        q = 2.0 * np.sqrt(1.0 - s[ok])
+        out[idx, 0] = x1[ok] * q
+        out[idx, 1] = x2[ok] * q
+        out[idx, 2] = 1.0 - 2.0 * s[ok]
+        todo = todo[~ok]
+    return out
+
+
 def plummer(n: int, seed: int = 0, a: float = 1.0, rmax: float = 20.0):
     rng = np.random.default_rng(seed)
     r = np.empty(n)
     todo = np.arange(n)
     while len(todo):
-        u = rng.uniform(0.0, 1.0, len(todo))
-        u = np.where(u <= 0.0, np.finfo(float).tiny, u)
-        rr = a / np.sqrt(u ** (-2.0 / 3.0) - 1.0)
-        ok = rr <= rmax * a
+        k = len(todo)
+        v = np.maximum(np.maximum(rng.uniform(0.0, 1.0, k), rng.uniform(0.0, 1.0, k)),
+                       rng.uniform(0.0, 1.0, k))          # v = u^(1/3)
+        ok = (v > 0.0) & (v < 1.0)
+        rr = np.full(k, np.inf)
+        rr[ok] = a * v[ok] / np.sqrt(1.0 - v[ok] * v[ok])
+        ok &= rr <= rmax * a
         r[todo[ok]] = rr[ok]
         todo = todo[~ok]
-    pos = _isotropic(rng, n) * r[:, None]
+    pos = _marsaglia_directions(rng, n) * r[:, None]
     return pos, np.full(n, 1.0 / n)
 
 
