@@ -52,6 +52,7 @@ SIGNATURES = {
     "bhut_morton_keys": (_INT, [_VP, _I64, _INT, _VP, _VP]),
     "bhut_morton_argsort": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),
     "bhut_direct_accelerations": (_INT, [_VP, _VP, _I64, _INT, _VP, _I64, _D, _D, _VP, _VP]),
+    "bhut_morton_argsort_noalloc": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),
 }
 
 _lock = threading.Lock()

@@ -120,6 +120,18 @@ BHUT_API int bhut_morton_keys(const double *positions, int64_t n, int dim, uint6
 BHUT_API int bhut_morton_argsort(const double *positions, int64_t n, int dim, uint64_t *sorted_keys,
                         int64_t *perm, void *stream);
 
+/* Morton keys + stable argsort that allocates no device memory.  No
+ * counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc (GPU memory owned by another allocator, or a step loop where an
+ * allocation would synchronize the device).  Same result as
+ * bhut_morton_argsort, with perm as int32.  All pointers must be device
+ * memory; n <= 1,048,576.  Scratch is one static device array (about 12.9 MB,
+ * held on every GPU that loads the library until exit) shared by all calls:
+ * calls that overlap on the GPU race.  The first call on a device looks up
+ * the array's address; make it before any stream capture. */
+BHUT_API int bhut_morton_argsort_noalloc(const double *positions, int64_t n, int dim,
+                                         uint64_t *sorted_keys, int32_t *perm, void *stream);
+
 /* FP64 direct sum (the theta = 0 limit) at m targets, or self accelerations
  * when targets == NULL (then m must equal n). */
 BHUT_API int bhut_direct_accelerations(const double *positions, const double *masses, int64_t n, int dim,
