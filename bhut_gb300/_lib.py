@@ -48,6 +48,7 @@ SIGNATURES = {
     "bhut_tree_destroy": (None, [_VP]),
     "bhut_tree_stats": (_INT, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                ctypes.POINTER(_I64)]),
+    "bhut_tree_fallbacks": (_INT, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "bhut_launch_count": (ctypes.c_longlong, []),
     "bhut_morton_keys": (_INT, [_VP, _I64, _INT, _VP, _VP]),
     "bhut_morton_argsort": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),

@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _lib
 
-DEFAULT_FORM = "exact"
+DEFAULT_FORM = "fast"
 
 
 # ---------------------------------------------------------------------------
@@ -243,6 +243,12 @@ class _Handle:
         _lib.check(self.L.bhut_tree_stats(self.h, ctypes.byref(a), ctypes.byref(b),
                                           ctypes.byref(c)))
         return a.value, b.value, c.value
+
+    def fallbacks(self):
+        """(exact opening decisions, FP64 pairs) of the last fast traversal."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(self.L.bhut_tree_fallbacks(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def info(self):
         n, m = ctypes.c_int64(), ctypes.c_int64()

@@ -28,10 +28,12 @@ namespace bhut {
 constexpr int kBoxThreads = 256;
 
 __global__ void __launch_bounds__(kBoxThreads)
-k_bbox(const double* __restrict__ pos, int64_t n, int dim, double* __restrict__ partial,
-       unsigned* __restrict__ done_counter, double* __restrict__ box, unsigned* __restrict__ err)
+k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t n, int dim,
+       double* __restrict__ partial, unsigned* __restrict__ done_counter, double* __restrict__ box,
+       unsigned* __restrict__ err)
 {
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    double mmax = 0.0;
     bool bad = false;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -41,7 +43,18 @@ k_bbox(const double* __restrict__ pos, int64_t n, int dim, double* __restrict__ 
             lo[d] = v < lo[d] ? v : lo[d];
             hi[d] = v > hi[d] ? v : hi[d];
         }
+        if (mass) {
+            double am = fabs(mass[i]);
+            bad |= !isfinite(am);
+            mmax = am > mmax ? am : mmax;
+        }
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        double a = __shfl_down_sync(0xffffffffu, mmax, o);
+        mmax = a > mmax ? a : mmax;
+    }
+    __shared__ double s_m[kBoxThreads / 32];
+    if ((threadIdx.x & 31) == 0) s_m[threadIdx.x >> 5] = mmax;
     __shared__ double s_lo[3][kBoxThreads / 32], s_hi[3][kBoxThreads / 32];
     __shared__ bool s_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -63,9 +76,12 @@ k_bbox(const double* __restrict__ pos, int64_t n, int dim, double* __restrict__ 
                 a = s_lo[d][w] < a ? s_lo[d][w] : a;
                 b = s_hi[d][w] > b ? s_hi[d][w] : b;
             }
-            partial[blockIdx.x * 6 + d] = a;
-            partial[blockIdx.x * 6 + 3 + d] = b;
+            partial[blockIdx.x * 8 + d] = a;
+            partial[blockIdx.x * 8 + 3 + d] = b;
         }
+        double mm = s_m[0];
+        for (int w = 1; w < kBoxThreads / 32; w++) mm = s_m[w] > mm ? s_m[w] : mm;
+        partial[blockIdx.x * 8 + 6] = mm;
         __threadfence();
         unsigned ticket = atomicAdd(done_counter, 1u);
         s_last = (ticket == gridDim.x - 1);
@@ -76,13 +92,19 @@ k_bbox(const double* __restrict__ pos, int64_t n, int dim, double* __restrict__ 
         for (int d = 0; d < 3; d++) {
             double a = __ldcg(&partial[d]), b = __ldcg(&partial[3 + d]);
             for (unsigned g = 1; g < gridDim.x; g++) {
-                double x = __ldcg(&partial[g * 6 + d]), y = __ldcg(&partial[g * 6 + 3 + d]);
+                double x = __ldcg(&partial[g * 8 + d]), y = __ldcg(&partial[g * 8 + 3 + d]);
                 a = x < a ? x : a;
                 b = y > b ? y : b;
             }
             box[d] = a;
             box[3 + d] = b;
         }
+        double mm = __ldcg(&partial[6]);
+        for (unsigned g = 1; g < gridDim.x; g++) {
+            double x = __ldcg(&partial[g * 8 + 6]);
+            mm = x > mm ? x : mm;
+        }
+        box[6] = mm;
         *done_counter = 0;
     }
 }
@@ -482,11 +504,11 @@ int make_topo_tables(int64_t n, int leaf_size, TopoTables* t)
     return kOk;
 }
 
-int launch_bbox(const double* pos, int64_t n, int dim, double* partial, unsigned* counter,
-                double* box, unsigned* err, cudaStream_t s)
+int launch_bbox(const double* pos, const double* mass, int64_t n, int dim, double* partial,
+                unsigned* counter, double* box, unsigned* err, cudaStream_t s)
 {
-    unsigned g = grid_for(n, kBoxThreads, 152u * 4u);
-    k_bbox<<<g, kBoxThreads, 0, s>>>(pos, n, dim, partial, counter, box, err);
+    unsigned g = grid_for(n, kBoxThreads, kBoxMaxBlocks);
+    k_bbox<<<g, kBoxThreads, 0, s>>>(pos, mass, n, dim, partial, counter, box, err);
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
     return kOk;

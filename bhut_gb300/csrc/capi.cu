@@ -108,9 +108,12 @@ struct bhut_tree {
     DevBuf cm, size, center, half, lo, hi, first_child, start, count, parent, leaf_list, arrive;
     // scratch
     DevBuf sort_scratch, box_partial, box, counters, err, stats;
-    unsigned long long last_stats[3] = {0, 0, 0};
+    unsigned long long last_stats[5] = {0, 0, 0, 0, 0};
     // traversal targets
     DevBuf tpos, tkeys, tperm, tx, ty, tz, tbox, out;
+    // float-float copies for the fast form
+    DevBuf frame, ph, pl, nh, nl, nsize, th, tl;
+    bool ff_valid = false;
 
     TreeDev dev() const
     {
@@ -157,16 +160,16 @@ int check_err_word(bhut_tree* t, const char* what)
 
 // Morton keys + stable sort of `n` AoS points into keys/perm (perm is the
 // sort payload, original index).  Uses the handle's scratch.
-int sort_points(bhut_tree* t, const double* dpos, int64_t n, DevBuf& keys, DevBuf& perm,
-                DevBuf& box)
+int sort_points(bhut_tree* t, const double* dpos, const double* dmass, int64_t n, DevBuf& keys,
+                DevBuf& perm, DevBuf& box)
 {
     cudaStream_t s = t->stream;
     BHUT_TRY(keys.ensure(sizeof(uint64_t) * n, s));
     BHUT_TRY(perm.ensure(sizeof(int32_t) * n, s));
-    BHUT_TRY(box.ensure(sizeof(double) * 6, s));
-    BHUT_TRY(t->box_partial.ensure(sizeof(double) * 6 * 152 * 4, s));
-    BHUT_TRY(launch_bbox(dpos, n, t->dim, t->box_partial.as<double>(), t->counters.as<unsigned>(),
-                         box.as<double>(), t->err.as<unsigned>(), s));
+    BHUT_TRY(box.ensure(sizeof(double) * kBoxDoubles, s));
+    BHUT_TRY(t->box_partial.ensure(sizeof(double) * kBoxPartialDoubles, s));
+    BHUT_TRY(launch_bbox(dpos, dmass, n, t->dim, t->box_partial.as<double>(),
+                         t->counters.as<unsigned>(), box.as<double>(), t->err.as<unsigned>(), s));
     BHUT_TRY(launch_morton(dpos, n, t->dim, box.as<double>(), keys.as<uint64_t>(),
                            perm.as<int32_t>(), s));
     BHUT_TRY(t->sort_scratch.ensure(sort_scratch_bytes(n), s));
@@ -186,7 +189,7 @@ int do_build(bhut_tree* t, int64_t n)
     t->n = n;
     t->m = t->tt.num_nodes;
     const int64_t m = t->m;
-    BHUT_TRY(sort_points(t, t->pos.as<double>(), n, t->keys, t->perm, t->box));
+    BHUT_TRY(sort_points(t, t->pos.as<double>(), t->mass.as<double>(), n, t->keys, t->perm, t->box));
     for (DevBuf* b : {&t->sx, &t->sy, &t->sz, &t->sm}) BHUT_TRY(b->ensure(sizeof(double) * n, s));
     BHUT_TRY(launch_gather(t->pos.as<double>(), t->mass.as<double>(), t->perm.as<int32_t>(), n, dim,
                            t->sx.as<double>(), t->sy.as<double>(), t->sz.as<double>(),
@@ -212,6 +215,7 @@ int do_build(bhut_tree* t, int64_t n)
                               t->count.as<int32_t>(), t->parent.as<int32_t>(),
                               t->arrive.as<unsigned>(), t->nodes(), false, nullptr, nullptr,
                               t->err.as<unsigned>(), s));
+    t->ff_valid = false;
     int st = check_err_word(t, "build");
     if (st != kOk) {
         t->built = false;
@@ -269,21 +273,77 @@ int finish_out(bhut_tree* t, const OutTarget& o, size_t bytes, const char* what)
     return check_err_word(t, what);
 }
 
+// Float-float copies of particles and nodes for the fast form (built once
+// per build/refit, on first use).
+int prepare_fast(bhut_tree* t)
+{
+    if (t->ff_valid) return kOk;
+    cudaStream_t s = t->stream;
+    BHUT_TRY(t->frame.ensure(sizeof(FastFrame), s));
+    BHUT_TRY(t->ph.ensure(sizeof(float4) * t->n, s));
+    BHUT_TRY(t->pl.ensure(sizeof(float4) * t->n, s));
+    BHUT_TRY(t->nh.ensure(sizeof(float4) * t->m, s));
+    BHUT_TRY(t->nl.ensure(sizeof(float4) * t->m, s));
+    BHUT_TRY(t->nsize.ensure(sizeof(float) * t->m, s));
+    BHUT_TRY(launch_fast_prepare(t->box.as<double>(), t->dim, t->frame.as<FastFrame>(), t->dev(),
+                                 t->ph.as<float4>(), t->pl.as<float4>(), t->nh.as<float4>(),
+                                 t->nl.as<float4>(), t->nsize.as<float>(), s));
+    t->ff_valid = true;
+    return kOk;
+}
+
+FastTree fast_tree(const bhut_tree* t)
+{
+    return FastTree{t->frame.as<FastFrame>(), t->ph.as<float4>(), t->pl.as<float4>(),
+                    t->nh.as<float4>(), t->nl.as<float4>(), t->nsize.as<float>()};
+}
+
+// Scale of the fast form's normalised coordinates (the frame's s), read
+// back once per traversal to scale the softening.
+int frame_scale(bhut_tree* t, double* s_out)
+{
+    FastFrame f;
+    BHUT_CUDA(cudaMemcpyAsync(&f, t->frame.p, sizeof(FastFrame), cudaMemcpyDeviceToHost, t->stream));
+    BHUT_CUDA(cudaStreamSynchronize(t->stream));
+    *s_out = f.s;
+    return kOk;
+}
+
 int traverse(bhut_tree* t, const double* tx, const double* ty, const double* tz,
              const int32_t* self_id, const int32_t* out_idx, int64_t nt, double theta, double eps,
-             double G, double* out)
+             double G, double* out, bool self_targets)
 {
     TreeDev d = t->dev();
-    BHUT_TRY(t->stats.ensure(sizeof(unsigned long long) * 4, t->stream));
-    BHUT_CUDA(cudaMemsetAsync(t->stats.p, 0, sizeof(unsigned long long) * 4, t->stream));
+    BHUT_TRY(t->stats.ensure(sizeof(unsigned long long) * 8, t->stream));
+    BHUT_CUDA(cudaMemsetAsync(t->stats.p, 0, sizeof(unsigned long long) * 8, t->stream));
     unsigned long long* st = t->stats.as<unsigned long long>();
     switch (t->form) {
+    case BHUT_FORM_FAST: {
+        BHUT_TRY(prepare_fast(t));
+        double sc = 1.0;
+        BHUT_TRY(frame_scale(t, &sc));
+        const float4* th = nullptr;
+        const float4* tl = nullptr;
+        if (!self_targets) {
+            BHUT_TRY(t->th.ensure(sizeof(float4) * nt, t->stream));
+            BHUT_TRY(t->tl.ensure(sizeof(float4) * nt, t->stream));
+            BHUT_TRY(launch_fast_targets(tx, ty, tz, nt, t->dim, t->frame.as<FastFrame>(),
+                                         t->th.as<float4>(), t->tl.as<float4>(), t->stream));
+            th = t->th.as<float4>();
+            tl = t->tl.as<float4>();
+        }
+        const double es = eps * sc;
+        BHUT_TRY(launch_traverse_fast(d, fast_tree(t), th, tl, tx, ty, tz, self_id, out_idx, nt,
+                                      theta, eps, G, es * es, out, t->err.as<unsigned>(), st,
+                                      t->stream));
+        break;
+    }
     case BHUT_FORM_EXACT:
     default:
         BHUT_TRY(launch_traverse_exact(d, tx, ty, tz, self_id, out_idx, nt, theta, eps, G, out,
                                        t->err.as<unsigned>(), st, t->stream));
     }
-    BHUT_CUDA(cudaMemcpyAsync(t->last_stats, st, sizeof(unsigned long long) * 3,
+    BHUT_CUDA(cudaMemcpyAsync(t->last_stats, st, sizeof(unsigned long long) * 5,
                               cudaMemcpyDeviceToHost, t->stream));
     return kOk;
 }
@@ -385,13 +445,14 @@ int bhut_tree_refit(bhut_tree* t, const double* positions, const double* masses,
                               t->count.as<int32_t>(), t->parent.as<int32_t>(),
                               t->arrive.as<unsigned>(), t->nodes(), true, t->pos.as<double>(),
                               t->mass.as<double>(), t->err.as<unsigned>(), s));
+    t->ff_valid = false;
     return check_err_word(t, "refit");
 }
 
 int bhut_tree_set_form(bhut_tree* t, int form)
 {
     if (!t) { set_error("tree is NULL"); return kInvalid; }
-    if (form != BHUT_FORM_EXACT) {
+    if (form != BHUT_FORM_EXACT && form != BHUT_FORM_FAST) {
         set_error("traversal form %d is not available in this build", form);
         return kInvalid;
     }
@@ -411,7 +472,7 @@ int bhut_tree_accel_self(bhut_tree* t, double theta, double softening, double G,
     BHUT_TRY(out_target(t, out, bytes, &o));
     BHUT_TRY(traverse(t, t->sx.as<double>(), t->sy.as<double>(), t->sz.as<double>(),
                       t->perm.as<int32_t>(), t->perm.as<int32_t>(), t->n, theta, softening, G,
-                      o.dev));
+                      o.dev, true));
     return finish_out(t, o, bytes, "accelerations");
 }
 
@@ -431,7 +492,7 @@ int bhut_tree_accel_targets(bhut_tree* t, const double* targets, int64_t mt, dou
     BHUT_TRY(stage_in(t->tpos, targets, bytes, s));
     // Morton-order the targets (their own box) so each warp's 32 targets are
     // close together; results are scattered back to input order.
-    BHUT_TRY(sort_points(t, t->tpos.as<double>(), mt, t->tkeys, t->tperm, t->tbox));
+    BHUT_TRY(sort_points(t, t->tpos.as<double>(), nullptr, mt, t->tkeys, t->tperm, t->tbox));
     for (DevBuf* b : {&t->tx, &t->ty, &t->tz}) BHUT_TRY(b->ensure(sizeof(double) * mt, s));
     BHUT_TRY(launch_gather(t->tpos.as<double>(), nullptr, t->tperm.as<int32_t>(), mt, dim,
                            t->tx.as<double>(), t->ty.as<double>(), t->tz.as<double>(), nullptr, s));
@@ -440,7 +501,7 @@ int bhut_tree_accel_targets(bhut_tree* t, const double* targets, int64_t mt, dou
     OutTarget o;
     BHUT_TRY(out_target(t, out, bytes, &o));
     BHUT_TRY(traverse(t, t->tx.as<double>(), t->ty.as<double>(), t->tz.as<double>(), nullptr,
-                      t->tperm.as<int32_t>(), mt, theta, softening, G, o.dev));
+                      t->tperm.as<int32_t>(), mt, theta, softening, G, o.dev, false));
     return finish_out(t, o, bytes, "accelerations at targets");
 }
 
@@ -450,6 +511,14 @@ int bhut_tree_stats(const bhut_tree* t, int64_t* p2p, int64_t* m2p, int64_t* vis
     if (p2p) *p2p = (int64_t)t->last_stats[0];
     if (m2p) *m2p = (int64_t)t->last_stats[1];
     if (visits) *visits = (int64_t)t->last_stats[2];
+    return kOk;
+}
+
+int bhut_tree_fallbacks(const bhut_tree* t, int64_t* exact_decisions, int64_t* fp64_pairs)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (exact_decisions) *exact_decisions = (int64_t)t->last_stats[3];
+    if (fp64_pairs) *fp64_pairs = (int64_t)t->last_stats[4];
     return kOk;
 }
 
@@ -518,7 +587,8 @@ void bhut_tree_destroy(bhut_tree* t)
                      &t->cm, &t->size, &t->center, &t->half, &t->lo, &t->hi, &t->first_child,
                      &t->start, &t->count, &t->parent, &t->leaf_list, &t->arrive,
                      &t->sort_scratch, &t->box_partial, &t->box, &t->counters, &t->err, &t->stats,
-                     &t->tpos, &t->tkeys, &t->tperm, &t->tx, &t->ty, &t->tz, &t->tbox, &t->out};
+                     &t->tpos, &t->tkeys, &t->tperm, &t->tx, &t->ty, &t->tz, &t->tbox, &t->out,
+                     &t->frame, &t->ph, &t->pl, &t->nh, &t->nl, &t->nsize, &t->th, &t->tl};
     for (DevBuf* b : all) b->release(s);
     cudaStreamSynchronize(s);
     if (t->own_stream) cudaStreamDestroy(s);
@@ -532,10 +602,10 @@ int bhut_morton_keys(const double* positions, int64_t n, int dim, uint64_t* keys
     bhut_tree* t = nullptr;
     BHUT_TRY(bhut_tree_create(dim, 1, stream, &t));
     int rc = stage_in(t->pos, positions, sizeof(double) * n * dim, t->stream);
-    if (rc == kOk) rc = t->box.ensure(sizeof(double) * 6, t->stream);
-    if (rc == kOk) rc = t->box_partial.ensure(sizeof(double) * 6 * 152 * 4, t->stream);
+    if (rc == kOk) rc = t->box.ensure(sizeof(double) * kBoxDoubles, t->stream);
+    if (rc == kOk) rc = t->box_partial.ensure(sizeof(double) * kBoxPartialDoubles, t->stream);
     if (rc == kOk) rc = t->keys.ensure(sizeof(uint64_t) * n, t->stream);
-    if (rc == kOk) rc = launch_bbox(t->pos.as<double>(), n, dim, t->box_partial.as<double>(),
+    if (rc == kOk) rc = launch_bbox(t->pos.as<double>(), nullptr, n, dim, t->box_partial.as<double>(),
                                     t->counters.as<unsigned>(), t->box.as<double>(),
                                     t->err.as<unsigned>(), t->stream);
     if (rc == kOk) rc = launch_morton(t->pos.as<double>(), n, dim, t->box.as<double>(),
@@ -558,7 +628,7 @@ int bhut_morton_argsort(const double* positions, int64_t n, int dim, uint64_t* s
     bhut_tree* t = nullptr;
     BHUT_TRY(bhut_tree_create(dim, 1, stream, &t));
     int rc = stage_in(t->pos, positions, sizeof(double) * n * dim, t->stream);
-    if (rc == kOk) rc = sort_points(t, t->pos.as<double>(), n, t->keys, t->perm, t->box);
+    if (rc == kOk) rc = sort_points(t, t->pos.as<double>(), nullptr, n, t->keys, t->perm, t->box);
     int32_t* p32 = nullptr;
     if (rc == kOk && sorted_keys) {
         cudaError_t e = cudaMemcpyAsync(sorted_keys, t->keys.p, sizeof(uint64_t) * n,

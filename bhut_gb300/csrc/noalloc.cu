@@ -44,7 +44,7 @@ constexpr size_t kSortBytes = align256(sizeof(uint64_t) * kNoAllocMaxPoints) +
                               align256(sizeof(int32_t) * kNoAllocMaxPoints) +
                               align256(sizeof(uint32_t) * kMaxCounts) +
                               align256(sizeof(uint32_t) * (kMaxCounts / 4096 + 2));
-constexpr size_t kBoxPartialBytes = align256(sizeof(double) * 6 * 152 * 4);
+constexpr size_t kBoxPartialBytes = align256(sizeof(double) * kBoxPartialDoubles);
 constexpr size_t kBoxBytes = 256;
 constexpr size_t kWordBytes = 256;                      // counters[8] + error word
 constexpr size_t kScratchBytes = kSortBytes + kBoxPartialBytes + kBoxBytes + kWordBytes;
@@ -112,7 +112,7 @@ extern "C" int bhut_morton_argsort_noalloc(const double* positions, int64_t n, i
     unsigned* counter = words;        // bbox last-block counter
     unsigned* err = words + 8;        // error word
     BHUT_CUDA(cudaMemsetAsync(words, 0, kWordBytes, s));
-    BHUT_TRY(launch_bbox(positions, n, dim, box_partial, counter, box, err, s));
+    BHUT_TRY(launch_bbox(positions, nullptr, n, dim, box_partial, counter, box, err, s));
     BHUT_TRY(launch_morton(positions, n, dim, box, sorted_keys, perm, s));
     BHUT_TRY(radix_sort_pairs(sorted_keys, perm, n, dim == 3 ? 63 : 42, sort_region, s));
     unsigned e = 0;

@@ -1,0 +1,504 @@
+// Barnes-Hut traversal, form "fast": FP64-accurate results from float-float
+// arithmetic on the FP32 pipe.
+//
+// On GB300 the FP64 pipe runs at about 1/70 of the FP32 pipe, and f32<->f64
+// conversions at the FP64 rate, so the FP64 pair loop of k_traverse_exact is
+// bound at ~1 TFLOP/s.  This kernel keeps every pair term to ~2^-44 relative
+// (the sum of ~5e4 such terms is far inside the 1e-10 relative-L2 contract)
+// while issuing only FP32 instructions in the hot loop:
+//
+//  * Coordinates are shifted to the tree's box centre and scaled by a power
+//    of two into [-1/2, 1/2]; each coordinate is stored as hi + lo where hi lies
+//    on the 2^-23 grid (so hi_j - hi_i is exact in FP32) and lo is the FP32
+//    rounding of the remainder (|lo| <= 2^-24).  Masses are scaled by a power
+//    of two into [-1, 1] and split hi + lo.  Scales are undone in FP64.
+//  * r^2 + eps^2 is summed error-free (two-product squares, TwoSum of the
+//    high parts); (r^2)^(-3/2) is the hardware rsqrt refined by one
+//    correction step, w = y^3 (1 + 3e/2 + 15e^2/8) with e = 1 - r^2 y^2
+//    computed exactly (Newton-Raphson for the inverse square root, carried
+//    to second order); m * w * dx and the accumulation are float-float
+//    (Dekker/Knuth two-product and TwoSum).
+//  * Pairs closer than 2^-15 in normalised units (2^-14 of the box
+//    half-size), or outside the FP32 range, are evaluated in FP64 from the
+//    FP64 arrays instead.
+//  * The opening decision is the reference's, bit for bit: a FP32 test
+//    decides every node whose ratio is clearly above or below theta, and
+//    nodes inside a small error band are decided by the exact FP64 test of
+//    k_traverse_exact (bh.py:576-601).  Every lane therefore evaluates
+//    exactly the reference's interaction set for its target.
+#include "tree.cuh"
+
+namespace bhut {
+
+constexpr int kFastWarps = 4;
+constexpr int kFastThreads = kFastWarps * kWarp;
+constexpr float kTinyR = 0x1p-30f;     // r^2 below this (normalised) -> FP64 pair
+constexpr float kHugeR = 0x1p+100f;    // r^2 above this -> FP64 pair
+constexpr float kBandRel = 0x1p-18f;   // opening-test error band, relative part
+constexpr float kBandAbs = 0x1p-21f;   // ... absolute part per unit of (1 + |target|)
+
+// ---------------------------------------------------------------------------
+// frame (normalisation) derived from the tree's bounding box
+// ---------------------------------------------------------------------------
+__device__ void frame_from_box(const double* box, int dim, FastFrame* f)
+{
+    double h = 0.0;
+    for (int d = 0; d < 3; d++) f->c[d] = 0.0;
+    for (int d = 0; d < dim; d++) {
+        f->c[d] = __dmul_rn(__dadd_rn(box[d], box[3 + d]), 0.5);
+        double e = __dmul_rn(__dsub_rn(box[3 + d], box[d]), 0.5);
+        h = e > h ? e : h;
+    }
+    if (!(h > 0.0)) h = 1.0;
+    // Map the box into [-1/2, 1/2]: a refit may move particles to 1.1x the
+    // root box (bhut/tree/refit.py:236-249) and targets inside [-1, 1] are
+    // still on the grid; every hi difference then stays below 2 and is exact.
+    int ex;
+    frexp(h, &ex);                      // h <= 2^ex
+    f->s = ldexp(1.0, -ex - 1);
+    double mm = box[6];
+    int em = 0;
+    if (mm > 0.0) frexp(mm, &em);       // |m| <= 2^em
+    f->ms = ldexp(1.0, -em);
+    f->conv = ldexp(1.0, em - 2 * ex - 2);  // normalised -> physical acceleration (s^2 / ms)
+}
+
+__global__ void k_frame(const double* __restrict__ box, int dim, FastFrame* __restrict__ f)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) frame_from_box(box, dim, f);
+}
+
+// hi on the 2^-23 grid (exact in FP32 for |u| <= 1), lo = fl32(u - hi).
+__device__ __forceinline__ void split_grid(double u, float& h, float& l)
+{
+    double H = rint(__dmul_rn(u, 8388608.0));
+    double hd = __dmul_rn(H, 1.0 / 8388608.0);
+    h = __double2float_rn(hd);
+    l = __double2float_rn(__dsub_rn(u, hd));
+}
+
+__device__ __forceinline__ void split_plain(double u, float& h, float& l)
+{
+    h = __double2float_rn(u);
+    l = __double2float_rn(__dsub_rn(u, (double)h));
+}
+
+__global__ void k_ff_particles(const double* __restrict__ sx, const double* __restrict__ sy,
+                               const double* __restrict__ sz, const double* __restrict__ sm,
+                               int64_t n, int dim, const FastFrame* __restrict__ fr,
+                               float4* __restrict__ ph, float4* __restrict__ pl)
+{
+    const FastFrame f = *fr;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float4 h, l;
+        split_grid(__dmul_rn(__dsub_rn(sx[i], f.c[0]), f.s), h.x, l.x);
+        split_grid(__dmul_rn(__dsub_rn(sy[i], f.c[1]), f.s), h.y, l.y);
+        if (dim == 3) split_grid(__dmul_rn(__dsub_rn(sz[i], f.c[2]), f.s), h.z, l.z);
+        else h.z = l.z = 0.0f;
+        split_plain(__dmul_rn(sm[i], f.ms), h.w, l.w);
+        ph[i] = h;
+        pl[i] = l;
+    }
+}
+
+__global__ void k_ff_nodes(const NodeCM* __restrict__ cm, const double* __restrict__ size,
+                           int64_t m, int dim, const FastFrame* __restrict__ fr,
+                           float4* __restrict__ nh, float4* __restrict__ nl,
+                           float* __restrict__ nsize)
+{
+    const FastFrame f = *fr;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        NodeCM c = cm[k];
+        float4 h, l;
+        // a node's COM lies inside the box: |u| <= 1 up to rounding
+        split_grid(__dmul_rn(__dsub_rn(c.x, f.c[0]), f.s), h.x, l.x);
+        split_grid(__dmul_rn(__dsub_rn(c.y, f.c[1]), f.s), h.y, l.y);
+        if (dim == 3) split_grid(__dmul_rn(__dsub_rn(c.z, f.c[2]), f.s), h.z, l.z);
+        else h.z = l.z = 0.0f;
+        split_plain(__dmul_rn(c.w, f.ms), h.w, l.w);
+        nh[k] = h;
+        nl[k] = l;
+        nsize[k] = __double2float_rn(__dmul_rn(size[k], f.s));
+    }
+}
+
+// Targets: grid split when inside the box (|u| <= 1), plain split otherwise;
+// th.w = 1 marks a target outside the box, tl.w = max |u|.
+__global__ void k_ff_targets(const double* __restrict__ tx, const double* __restrict__ ty,
+                             const double* __restrict__ tz, int64_t nt, int dim,
+                             const FastFrame* __restrict__ fr, float4* __restrict__ th,
+                             float4* __restrict__ tl)
+{
+    const FastFrame f = *fr;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nt;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double u[3] = {__dmul_rn(__dsub_rn(tx[i], f.c[0]), f.s),
+                       __dmul_rn(__dsub_rn(ty[i], f.c[1]), f.s),
+                       dim == 3 ? __dmul_rn(__dsub_rn(tz[i], f.c[2]), f.s) : 0.0};
+        double amax = fmax(fabs(u[0]), fmax(fabs(u[1]), fabs(u[2])));
+        bool inside = amax <= 1.0;
+        float hh[3], ll[3];
+        for (int d = 0; d < 3; d++) {
+            if (inside) split_grid(u[d], hh[d], ll[d]);
+            else split_plain(u[d], hh[d], ll[d]);
+        }
+        th[i] = make_float4(hh[0], hh[1], hh[2], inside ? 0.0f : 1.0f);
+        tl[i] = make_float4(ll[0], ll[1], ll[2], __double2float_ru(amax));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// float-float pair term
+// ---------------------------------------------------------------------------
+// Error of s = fl(a + b) (Knuth's TwoSum).
+__device__ __forceinline__ float two_sum_err(float a, float b, float s)
+{
+    float bb = __fsub_rn(s, a);
+    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ float comp(const float4& v, int k)
+{
+    return k == 0 ? v.x : (k == 1 ? v.y : v.z);
+}
+
+// Adds G-less m * (x_src - x_tgt) / (|dx|^2 + eps^2)^(3/2), normalised
+// units, to (ah, al).  Returns false when the pair must go to FP64.
+template <int DIM, bool FAR>
+__device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4 sh, float4 sl,
+                                        float e2h, float e2l, float* ah, float* al)
+{
+    float gh[3], gl[3];
+#pragma unroll
+    for (int k = 0; k < DIM; k++) {
+        float xh = comp(sh, k), xl = comp(sl, k);
+        float d = __fsub_rn(xh, Th[k]);              // exact on the grid
+        float l = __fsub_rn(xl, Tl[k]);
+        if (FAR) l = __fadd_rn(l, two_sum_err(xh, -Th[k], d));
+        float h = __fadd_rn(d, l);                   // FastTwoSum(d, l), |l| <= |d|
+        gl[k] = __fsub_rn(l, __fsub_rn(h, d));
+        gh[k] = h;
+    }
+    // R = |g|^2 + eps^2, error-free up to the cross term
+    float s = __fmul_rn(gh[0], gh[0]);
+    float lo = __fmaf_rn(gh[0], gh[0], -s);
+    float c = __fmul_rn(gh[0], gl[0]);
+#pragma unroll
+    for (int k = 1; k < DIM; k++) {
+        float p = __fmul_rn(gh[k], gh[k]);
+        float q = __fmaf_rn(gh[k], gh[k], -p);
+        float t = __fadd_rn(s, p);
+        lo = __fadd_rn(lo, __fadd_rn(two_sum_err(s, p, t), q));
+        s = t;
+        c = __fmaf_rn(gh[k], gl[k], c);
+    }
+    {
+        float t = __fadd_rn(s, e2h);
+        lo = __fadd_rn(lo, __fadd_rn(two_sum_err(s, e2h, t), e2l));
+        s = t;
+    }
+    lo = __fadd_rn(lo, __fadd_rn(c, c));
+    const float Rh = __fadd_rn(s, lo);
+    const float Rl = __fsub_rn(lo, __fsub_rn(Rh, s));
+    if (!(Rh >= kTinyR && Rh <= kHugeR)) return false;
+    // w = R^(-3/2): y ~ R^(-1/2); e = 1 - R y^2 exactly enough;
+    // w = y^3 (1 - e)^(-3/2) = y^3 (1 + 3e/2 + 15e^2/8 + O(e^3))
+    const float y = rsqrtf(Rh);
+    const float Y = __fmul_rn(y, y);
+    const float Ye = __fmaf_rn(y, y, -Y);
+    const float e = -__fmaf_rn(Rh, Ye, __fmaf_rn(Rl, Y, __fmaf_rn(Rh, Y, -1.0f)));
+    const float W = __fmul_rn(Y, y);
+    const float We = __fmaf_rn(Ye, y, __fmaf_rn(Y, y, -W));
+    const float corr = __fmul_rn(e, __fmaf_rn(1.875f, e, 1.5f));
+    const float wh = W;
+    const float wl = __fmaf_rn(W, corr, We);
+    // f = m w
+    const float fh = __fmul_rn(sh.w, wh);
+    const float fl = __fmaf_rn(sh.w, wl, __fmaf_rn(sl.w, wh, __fmaf_rn(sh.w, wh, -fh)));
+#pragma unroll
+    for (int k = 0; k < DIM; k++) {
+        float Fh = __fmul_rn(fh, gh[k]);
+        float Fl = __fmaf_rn(fh, gl[k], __fmaf_rn(fl, gh[k], __fmaf_rn(fh, gh[k], -Fh)));
+        float t = __fadd_rn(ah[k], Fh);
+        float err = two_sum_err(ah[k], Fh, t);
+        ah[k] = t;
+        al[k] = __fadd_rn(al[k], __fadd_rn(err, Fl));
+    }
+    return true;
+}
+
+// FP64 pair in physical units, G-less (the Numba loop arithmetic).
+template <int DIM>
+__device__ __forceinline__ void pair_fp64(double x, double y, double z, double px, double py,
+                                          double pz, double pm, double eps2, double* a64)
+{
+    const double dx = __dsub_rn(px, x), dy = __dsub_rn(py, y);
+    const double dz = DIM == 3 ? __dsub_rn(pz, z) : 0.0;
+    double r2 = __dmul_rn(dx, dx);
+    r2 = __dadd_rn(r2, __dmul_rn(dy, dy));
+    if (DIM == 3) r2 = __dadd_rn(r2, __dmul_rn(dz, dz));
+    r2 = __dadd_rn(r2, eps2);
+    if (r2 == 0.0) return;
+    const double ri = __ddiv_rn(1.0, __dsqrt_rn(r2));
+    const double f = __dmul_rn(pm, __dmul_rn(__dmul_rn(ri, ri), ri));
+    a64[0] = __dadd_rn(a64[0], __dmul_rn(f, dx));
+    a64[1] = __dadd_rn(a64[1], __dmul_rn(f, dy));
+    if (DIM == 3) a64[2] = __dadd_rn(a64[2], __dmul_rn(f, dz));
+}
+
+// Exact opening test (bh.py:576-601), same arithmetic as k_traverse_exact.
+template <int DIM>
+__device__ __forceinline__ bool open_exact64(double x, double y, double z, const NodeCM& cm,
+                                             double size, double theta)
+{
+    double dx = __dsub_rn(x, cm.x), dy = __dsub_rn(y, cm.y);
+    double s;
+    if (DIM == 3) {
+        double dz = __dsub_rn(z, cm.z);
+        s = __fma_rn(dz, dz, __fma_rn(dy, dy, __dmul_rn(dx, dx)));
+    } else {
+        s = __fma_rn(dy, dy, __dmul_rn(dx, dx));
+    }
+    double d = __dsqrt_rn(s);
+    if (d == 0.0) return true;
+    return __ddiv_rn(size, d) >= theta;
+}
+
+// ---------------------------------------------------------------------------
+// the traversal
+// ---------------------------------------------------------------------------
+struct FastArgs {
+    const float4* th;        // target hi (w: outside-box flag); NULL: the particles themselves
+    const float4* tl;        // target lo (w: max |u|)
+    const double* tx;        // target FP64 (fallbacks)
+    const double* ty;
+    const double* tz;
+    const int32_t* self_id;
+    const int32_t* out_idx;
+    int64_t nt;
+    double theta, eps, G;
+    float e2h, e2l;          // (eps * s)^2 as float-float
+    double* out;
+    unsigned* err;
+    unsigned long long* stats;
+};
+
+template <int DIM, bool FAR>
+__device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const FastArgs& a,
+                                     int w, int lane, bool valid, int32_t me, const float* Th,
+                                     const float* Tl, float band_abs, double x, double y, double z,
+                                     float* ah, float* al, double* a64, int2 (*stack)[kStackDepth],
+                                     float4 (*sh)[kWarp], float4 (*sl)[kWarp],
+                                     int32_t (*sid)[kWarp], unsigned long long* cnt, bool& overflow)
+{
+    const unsigned FULL = 0xffffffffu;
+    const float theta_f = (float)a.theta;
+    const double eps2 = __dmul_rn(a.eps, a.eps);
+    const unsigned live = __ballot_sync(FULL, valid);
+    if (lane == 0) stack[w][0] = make_int2(0, (int)live);
+    int sp = 1;
+    __syncwarp();
+    while (sp > 0) {
+        const int2 e = stack[w][--sp];
+        __syncwarp();
+        const int node = e.x;
+        const unsigned mask = (unsigned)e.y;
+        const bool act = (mask >> lane) & 1u;
+        cnt[2] += act;
+        const NodeCM cm = t.cm[node];
+        if (cm.w == 0.0) continue;                       // bh.py:514
+        const int fc = t.first_child[node];
+        if (fc < 0) {
+            const int s = t.start[node], c = t.count[node];
+            for (int b = 0; b < c; b += kWarp) {
+                const int jj = b + lane;
+                if (jj < c) {
+                    sh[w][lane] = ft.ph[s + jj];
+                    sl[w][lane] = ft.pl[s + jj];
+                    sid[w][lane] = t.perm[s + jj];
+                }
+                __syncwarp();
+                const int cn = min(kWarp, c - b);
+                if (act) {
+                    for (int q = 0; q < cn; q++) {
+                        if (sid[w][q] == me) continue;       // bh.py:254
+                        if (!pair_ff<DIM, FAR>(Th, Tl, sh[w][q], sl[w][q], a.e2h, a.e2l, ah, al)) {
+                            const int gi = s + b + q;
+                            pair_fp64<DIM>(x, y, z, t.sx[gi], t.sy[gi], DIM == 3 ? t.sz[gi] : 0.0,
+                                           t.sm[gi], eps2, a64);
+                            cnt[4]++;
+                        }
+                        cnt[0]++;
+                    }
+                }
+                __syncwarp();
+            }
+            if (act) {   // renormalise the accumulators once per leaf
+#pragma unroll
+                for (int k = 0; k < DIM; k++) {
+                    float hsum = __fadd_rn(ah[k], al[k]);
+                    al[k] = __fsub_rn(al[k], __fsub_rn(hsum, ah[k]));
+                    ah[k] = hsum;
+                }
+            }
+        } else {
+            bool open = false;
+            float4 nh = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (act) {
+                nh = ft.nh[node];
+                float d2 = 0.0f;
+#pragma unroll
+                for (int k = 0; k < DIM; k++) {
+                    float d = comp(nh, k) - Th[k];
+                    d2 = fmaf(d, d, d2);
+                }
+                const float dist = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+                const float td = theta_f * dist;
+                const float band = theta_f * fmaf(kBandRel, dist, band_abs);
+                const float size_f = ft.nsize[node];
+                if (size_f >= td + band) {
+                    open = true;
+                } else if (size_f < td - band) {
+                    open = false;
+                } else {
+                    open = open_exact64<DIM>(x, y, z, cm, t.size[node], a.theta);
+                    cnt[3]++;
+                }
+            }
+            const unsigned omask = __ballot_sync(FULL, act && open);
+            if (act && !open) {
+                const float4 nl = ft.nl[node];
+                if (!pair_ff<DIM, FAR>(Th, Tl, nh, nl, a.e2h, a.e2l, ah, al)) {
+                    pair_fp64<DIM>(x, y, z, cm.x, cm.y, cm.z, cm.w, eps2, a64);
+                    cnt[4]++;
+                }
+                cnt[1]++;
+            }
+            if (omask) {
+                if (sp + 2 > kStackDepth) { overflow = true; break; }
+                if (lane == 0) {
+                    stack[w][sp] = make_int2(fc, (int)omask);
+                    stack[w][sp + 1] = make_int2(fc + 1, (int)omask);
+                }
+                sp += 2;
+                __syncwarp();
+            }
+        }
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kFastThreads)
+k_traverse_fast(TreeDev t, FastTree ft, FastArgs a)
+{
+    __shared__ int2 stack[kFastWarps][kStackDepth];
+    __shared__ float4 sh[kFastWarps][kWarp], sl[kFastWarps][kWarp];
+    __shared__ int32_t sid[kFastWarps][kWarp];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned FULL = 0xffffffffu;
+    const FastFrame fr = *ft.frame;
+    const double conv = __dmul_rn(fr.conv, a.G);
+
+    for (int64_t base = ((int64_t)blockIdx.x * kFastWarps + w) * kWarp; base < a.nt;
+         base += (int64_t)gridDim.x * kFastWarps * kWarp) {
+        const int64_t i = base + lane;
+        const bool valid = i < a.nt;
+        float Th[3] = {0.f, 0.f, 0.f}, Tl[3] = {0.f, 0.f, 0.f};
+        bool far = false;
+        float amax = 0.f;
+        double x = 0.0, y = 0.0, z = 0.0;
+        int32_t me = -1;
+        if (valid) {
+            // self targets are the sorted particles themselves (inside the box)
+            const float4 h = a.th ? a.th[i] : ft.ph[i];
+            const float4 l = a.th ? a.tl[i] : ft.pl[i];
+            Th[0] = h.x; Th[1] = h.y; Th[2] = h.z;
+            Tl[0] = l.x; Tl[1] = l.y; Tl[2] = l.z;
+            far = a.th ? h.w != 0.0f : false;
+            amax = a.th ? l.w : 1.0f;
+            x = a.tx[i];
+            y = a.ty[i];
+            z = DIM == 3 ? a.tz[i] : 0.0;
+            me = a.self_id ? a.self_id[i] : -1;
+        }
+        const float band_abs = kBandAbs * (1.0f + amax);
+        float ah[3] = {0.f, 0.f, 0.f}, al[3] = {0.f, 0.f, 0.f};
+        double a64[3] = {0.0, 0.0, 0.0};
+        unsigned long long cnt[5] = {0, 0, 0, 0, 0};
+        bool overflow = false;
+        if (__any_sync(FULL, far))
+            walk<DIM, true>(t, ft, a, w, lane, valid, me, Th, Tl, band_abs, x, y, z, ah, al, a64,
+                            stack, sh, sl, sid, cnt, overflow);
+        else
+            walk<DIM, false>(t, ft, a, w, lane, valid, me, Th, Tl, band_abs, x, y, z, ah, al, a64,
+                             stack, sh, sl, sid, cnt, overflow);
+        if (overflow && lane == 0) atomicOr(a.err, kErrStackOverflow);
+        if (a.stats) {
+            for (int k = 0; k < 5; k++) {
+                unsigned long long v = cnt[k];
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+                if (lane == 0 && v) atomicAdd(&a.stats[k], v);
+            }
+        }
+        if (valid) {
+            const int64_t o = a.out_idx ? a.out_idx[i] : i;
+#pragma unroll
+            for (int k = 0; k < DIM; k++) {
+                double v = __dadd_rn((double)ah[k], (double)al[k]);
+                a.out[o * DIM + k] = __dadd_rn(__dmul_rn(v, conv), __dmul_rn(a64[k], a.G));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+int launch_fast_prepare(const double* box, int dim, FastFrame* frame, const TreeDev& t,
+                        float4* ph, float4* pl, float4* nh, float4* nl, float* nsize,
+                        cudaStream_t s)
+{
+    k_frame<<<1, 32, 0, s>>>(box, dim, frame);
+    k_ff_particles<<<grid_for(t.n, 256), 256, 0, s>>>(t.sx, t.sy, t.sz, t.sm, t.n, dim, frame, ph,
+                                                      pl);
+    k_ff_nodes<<<grid_for(t.m, 256), 256, 0, s>>>(t.cm, t.size, t.m, dim, frame, nh, nl, nsize);
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(3);
+    return kOk;
+}
+
+int launch_fast_targets(const double* tx, const double* ty, const double* tz, int64_t nt, int dim,
+                        const FastFrame* frame, float4* th, float4* tl, cudaStream_t s)
+{
+    k_ff_targets<<<grid_for(nt, 256), 256, 0, s>>>(tx, ty, tz, nt, dim, frame, th, tl);
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
+    return kOk;
+}
+
+int launch_traverse_fast(const TreeDev& t, const FastTree& ft, const float4* th, const float4* tl,
+                         const double* tx, const double* ty, const double* tz,
+                         const int32_t* self_id, const int32_t* out_idx, int64_t nt, double theta,
+                         double eps, double G, double eps_scaled_sq, double* out, unsigned* err,
+                         unsigned long long* stats, cudaStream_t s)
+{
+    if (nt <= 0) return kOk;
+    FastArgs a;
+    a.th = th; a.tl = tl; a.tx = tx; a.ty = ty; a.tz = tz;
+    a.self_id = self_id; a.out_idx = out_idx; a.nt = nt;
+    a.theta = theta; a.eps = eps; a.G = G;
+    a.e2h = (float)eps_scaled_sq;
+    a.e2l = (float)(eps_scaled_sq - (double)a.e2h);
+    a.out = out; a.err = err; a.stats = stats;
+    int64_t warps = (nt + kWarp - 1) / kWarp;
+    unsigned grid = grid_for(warps, kFastWarps, 152u * 64u);
+    if (t.dim == 3) k_traverse_fast<3><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+    else k_traverse_fast<2><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
+    return kOk;
+}
+
+}  // namespace bhut

@@ -48,6 +48,26 @@ struct TopoTables {
 
 int make_topo_tables(int64_t n, int leaf_size, TopoTables* t);
 
+// Normalisation of the "fast" traversal: u = (x - c) * s with s a power of
+// two mapping the box into [-1, 1]; masses scaled by ms (a power of two);
+// physical acceleration = normalised acceleration * conv (= s^2 / ms).
+struct FastFrame {
+    double c[3];
+    double s;
+    double ms;
+    double conv;
+};
+
+// Float-float copies of the particles (Morton order) and nodes.
+struct FastTree {
+    const FastFrame* frame;
+    const float4* ph;   // (x, y, z, m) hi
+    const float4* pl;   // (x, y, z, m) lo
+    const float4* nh;   // (com, mass) hi per node
+    const float4* nl;   // (com, mass) lo per node
+    const float* nsize; // 2 * half_size, normalised, per node
+};
+
 // Node arrays written by the bottom-up pass.
 struct NodeOut {
     NodeCM* cm;        // (com, mass)
@@ -59,8 +79,13 @@ struct NodeOut {
 };
 
 // Kernel launchers (build.cu, traverse.cu).
-int launch_bbox(const double* pos, int64_t n, int dim, double* partial, unsigned* counter,
-                double* box, unsigned* err, cudaStream_t s);
+// Bounding box: box[0..2] = min, box[3..5] = max, box[6] = max |mass| (0
+// without masses).  `partial` holds kBoxPartialDoubles doubles.
+constexpr unsigned kBoxMaxBlocks = 152u * 4u;
+constexpr int kBoxPartialDoubles = 8 * (int)kBoxMaxBlocks;
+constexpr int kBoxDoubles = 8;
+int launch_bbox(const double* pos, const double* mass, int64_t n, int dim, double* partial,
+                unsigned* counter, double* box, unsigned* err, cudaStream_t s);
 int launch_morton(const double* pos, int64_t n, int dim, const double* box, uint64_t* keys,
                   int32_t* idx, cudaStream_t s);
 int launch_gather(const double* pos, const double* mass, const int32_t* perm, int64_t n, int dim,
@@ -78,6 +103,16 @@ int launch_traverse_exact(const TreeDev& t, const double* tx, const double* ty, 
                           const int32_t* self_id, const int32_t* out_idx, int64_t nt, double theta,
                           double eps, double G, double* out, unsigned* err,
                           unsigned long long* stats, cudaStream_t s);
+int launch_fast_prepare(const double* box, int dim, FastFrame* frame, const TreeDev& t,
+                        float4* ph, float4* pl, float4* nh, float4* nl, float* nsize,
+                        cudaStream_t s);
+int launch_fast_targets(const double* tx, const double* ty, const double* tz, int64_t nt, int dim,
+                        const FastFrame* frame, float4* th, float4* tl, cudaStream_t s);
+int launch_traverse_fast(const TreeDev& t, const FastTree& ft, const float4* th, const float4* tl,
+                         const double* tx, const double* ty, const double* tz,
+                         const int32_t* self_id, const int32_t* out_idx, int64_t nt, double theta,
+                         double eps, double G, double eps_scaled_sq, double* out, unsigned* err,
+                         unsigned long long* stats, cudaStream_t s);
 int launch_direct(const double* pos, const double* mass, int64_t n, int dim, const double* targets,
                   const int64_t* self_id, int64_t nt, double eps, double G, double* out,
                   cudaStream_t s);

@@ -95,6 +95,11 @@ BHUT_API int bhut_tree_set_form(bhut_tree *t, int form);
  * target itself and zero-distance pairs are not counted). */
 BHUT_API int bhut_tree_stats(const bhut_tree *t, int64_t *p2p, int64_t *m2p, int64_t *visits);
 
+/* Fallbacks of the last fast-form traversal: opening decisions that fell in
+ * the FP32 test's error band and were taken by the exact FP64 test, and
+ * pairs evaluated in FP64 (closer than 2^-15 of the box half-size). */
+BHUT_API int bhut_tree_fallbacks(const bhut_tree *t, int64_t *exact_decisions, int64_t *fp64_pairs);
+
 /* Total number of kernels this library has launched in the process. */
 BHUT_API long long bhut_launch_count(void);
 
