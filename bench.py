@@ -200,12 +200,13 @@ def run_reference(args, ws, rank):
 # ---------------------------------------------------------------------------
 # GPU side
 # ---------------------------------------------------------------------------
-def measure_fp64_peak(torch) -> float:
-    """Measured FP64 throughput of this GPU: cuBLAS DGEMM (torch.matmul on
-    float64), best of 5, TFLOP/s."""
+def measure_gemm_peak(torch, dtype) -> float:
+    """Measured dense throughput of this GPU for one precision: cuBLAS GEMM
+    (torch.matmul, TF32 disabled for float32), 4096^3, best of 5, TFLOP/s."""
+    torch.backends.cuda.matmul.allow_tf32 = False
     n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    a = torch.randn(n, n, dtype=dtype, device="cuda")
+    b = torch.randn(n, n, dtype=dtype, device="cuda")
     for _ in range(2):
         a @ b
     torch.cuda.synchronize()
@@ -218,6 +219,14 @@ def measure_fp64_peak(torch) -> float:
         e1.synchronize()
         best = min(best, e0.elapsed_time(e1) / 1e3)
     return 2.0 * n ** 3 / best / 1e12
+
+
+# FP32-pipe operations of one float-float pair (or monopole) term of the fast
+# form, counted from bhut_gb300/csrc/traverse_fast.cu (pair_ff, 3-D, target
+# inside the box): displacement 15, r^2 + eps^2 43, range check 2, refined
+# rsqrt and cube 11, m * w 4, three float-float products and accumulations
+# 36 -> 107 (plus one MUFU rsqrt).
+FF_OPS_PER_INTERACTION = 107
 
 
 def run_ours(args, ws, rank, local):
@@ -251,6 +260,7 @@ def run_ours(args, ws, rank, local):
         step()
     torch.cuda.synchronize()
     p2p, m2p, visits = h.stats()
+    fb_dec, fb_pairs = h.fallbacks()
 
     clocks = ClockSampler(local)
     _barrier(ws)
@@ -291,11 +301,39 @@ def run_ours(args, ws, rank, local):
     if rank != 0:
         h.close()
         return
-    peak = measure_fp64_peak(torch)
+    peak64 = measure_gemm_peak(torch, torch.float64)
+    peak32 = measure_gemm_peak(torch, torch.float32)
     trav_s = trav_ms / 1e3 / args.steps
-    flops = FLOPS_PER_INTERACTION * (p2p + m2p)
-    achieved = flops / trav_s / 1e12
+    inter = p2p + m2p
+    flops = FLOPS_PER_INTERACTION * inter
+    achieved64 = flops / trav_s / 1e12
     traffic = _traffic_from_profile(args)
+    if args.form == "exact":
+        roofline = {
+            "bound": "fp64", "kernel": "k_traverse_exact", "achieved": achieved64,
+            "peak": peak64, "unit": "TFLOP/s", "frac": achieved64 / peak64, "traffic": traffic,
+            "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (MEASURED_PEAKS.json has "
+                           "no FP64 figure)",
+            "work_per_launch": flops,
+            "work_rule": f"{FLOPS_PER_INTERACTION} flop x (pair + monopole evaluations counted "
+                         "by the kernel)"}
+    else:
+        ops = FF_OPS_PER_INTERACTION * inter
+        achieved32 = ops / trav_s / 1e12
+        fma_rate = peak32 / 2.0      # FP32 pipe lane-instructions per second (one FMA = 2 flop)
+        roofline = {
+            "bound": "fp32", "kernel": "k_traverse_fast", "achieved": achieved32,
+            "peak": fma_rate, "unit": "T FP32-pipe ops/s", "frac": achieved32 / fma_rate,
+            "traffic": traffic,
+            "peak_source": "cuBLAS SGEMM 4096^3 (TF32 off) measured in this run, / 2 for the "
+                           "FMA-instruction rate (MEASURED_PEAKS.json has no FP32 figure)",
+            "work_per_launch": ops,
+            "work_rule": f"{FF_OPS_PER_INTERACTION} FP32 ops per float-float pair/monopole term "
+                         "x evaluations counted by the kernel",
+            "fp64_equivalent": {"achieved": achieved64, "peak": peak64, "unit": "TFLOP/s",
+                                "frac": achieved64 / peak64,
+                                "rule": f"{FLOPS_PER_INTERACTION} flop per interaction vs "
+                                        "measured DGEMM"}}
     line = {
         "metric": METRIC, "value": value, "unit": "accels/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
@@ -305,18 +343,11 @@ def run_ours(args, ws, rank, local):
                 "h2d_bytes_per_step": int(pos.nbytes + m.nbytes),
                 "d2h_bytes_per_step": int(n * 3 * 8), "api": "bhut_gb300.accelerations"},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "fp64", "kernel": "k_traverse_exact" if args.form == "exact"
-                     else f"traversal ({args.form})",
-                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None, "traffic": traffic,
-                     "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 pipe; "
-                                    "MEASURED_PEAKS.json has no FP64 figure)",
-                     "flops_per_launch": flops,
-                     "flop_rule": f"{FLOPS_PER_INTERACTION} x (pair + monopole evaluations) "
-                                  "counted by the kernel"},
+        "roofline": roofline,
         "traversal_ms": trav_s * 1e3,
         "build_ms": (total_ms - trav_ms) / args.steps,
-        "interactions_per_solve": {"p2p": p2p, "m2p": m2p, "node_visits": visits},
+        "interactions_per_solve": {"p2p": p2p, "m2p": m2p, "node_visits": visits,
+                                   "fp64_fallback_decisions": fb_dec, "fp64_pairs": fb_pairs},
         "clocks": clk,
     }
     if not args.no_cpu_baseline:

@@ -8,9 +8,10 @@
 // while issuing only FP32 instructions in the hot loop:
 //
 //  * Coordinates are shifted to the tree's box centre and scaled by a power
-//    of two into [-1/2, 1/2]; each coordinate is stored as hi + lo where hi lies
-//    on the 2^-23 grid (so hi_j - hi_i is exact in FP32) and lo is the FP32
-//    rounding of the remainder (|lo| <= 2^-24).  Masses are scaled by a power
+//    of two into [-1/2, 1/2]; each coordinate is stored as hi + lo with hi on
+//    the 2^-23 grid and lo on the 2^-47 grid (|lo| <= 2^-24), so hi_j - hi_i
+//    and lo_j - lo_i are exact in FP32 and the displacement is exact up to
+//    the 2^-48 representation of the coordinates.  Masses are scaled by a power
 //    of two into [-1, 1] and split hi + lo.  Scales are undone in FP64.
 //  * r^2 + eps^2 is summed error-free (two-product squares, TwoSum of the
 //    high parts); (r^2)^(-3/2) is the hardware rsqrt refined by one
@@ -32,6 +33,7 @@ namespace bhut {
 
 constexpr int kFastWarps = 4;
 constexpr int kFastThreads = kFastWarps * kWarp;
+constexpr int kFastBlocksPerSM = 6;    // 24 warps per SM: registers capped at 80
 constexpr float kTinyR = 0x1p-30f;     // r^2 below this (normalised) -> FP64 pair
 constexpr float kHugeR = 0x1p+100f;    // r^2 above this -> FP64 pair
 constexpr float kBandRel = 0x1p-18f;   // opening-test error band, relative part
@@ -68,13 +70,16 @@ __global__ void k_frame(const double* __restrict__ box, int dim, FastFrame* __re
     if (threadIdx.x == 0 && blockIdx.x == 0) frame_from_box(box, dim, f);
 }
 
-// hi on the 2^-23 grid (exact in FP32 for |u| <= 1), lo = fl32(u - hi).
+// hi on the 2^-23 grid and lo on the 2^-47 grid (both exact in FP32 for
+// |u| <= 1): differences of hi parts, and of lo parts, are then exact in
+// FP32; u is represented to within 2^-48.
 __device__ __forceinline__ void split_grid(double u, float& h, float& l)
 {
     double H = rint(__dmul_rn(u, 8388608.0));
     double hd = __dmul_rn(H, 1.0 / 8388608.0);
     h = __double2float_rn(hd);
-    l = __double2float_rn(__dsub_rn(u, hd));
+    double L = rint(__dmul_rn(__dsub_rn(u, hd), 140737488355328.0));   // 2^47
+    l = __double2float_rn(__dmul_rn(L, 1.0 / 140737488355328.0));
 }
 
 __device__ __forceinline__ void split_plain(double u, float& h, float& l)
@@ -166,6 +171,12 @@ __device__ __forceinline__ float comp(const float4& v, int k)
 
 // Adds G-less m * (x_src - x_tgt) / (|dx|^2 + eps^2)^(3/2), normalised
 // units, to (ah, al).  Returns false when the pair must go to FP64.
+//
+// d = hi_src - hi_tgt is exact on the grid and l = lo_src - lo_tgt is small
+// (|l| <= 2^-23), so (d, l) is renormalised with FastTwoSum into (gh, gl),
+// |gl| <= ulp(gh) / 2; every later product of a float-float with g then
+// keeps ~2^-47 relative accuracy.  A pair at zero displacement (the target
+// itself, or a duplicate) contributes exactly zero, as in the reference.
 template <int DIM, bool FAR>
 __device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4 sh, float4 sl,
                                         float e2h, float e2l, float* ah, float* al)
@@ -173,36 +184,39 @@ __device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4
     float gh[3], gl[3];
 #pragma unroll
     for (int k = 0; k < DIM; k++) {
-        float xh = comp(sh, k), xl = comp(sl, k);
-        float d = __fsub_rn(xh, Th[k]);              // exact on the grid
-        float l = __fsub_rn(xl, Tl[k]);
+        const float xh = comp(sh, k);
+        const float d = __fsub_rn(xh, Th[k]);        // exact on the grid
+        float l = __fsub_rn(comp(sl, k), Tl[k]);
         if (FAR) l = __fadd_rn(l, two_sum_err(xh, -Th[k], d));
-        float h = __fadd_rn(d, l);                   // FastTwoSum(d, l), |l| <= |d|
+        const float h = __fadd_rn(d, l);             // FastTwoSum(d, l), |l| <= |d| or d == 0
         gl[k] = __fsub_rn(l, __fsub_rn(h, d));
         gh[k] = h;
     }
-    // R = |g|^2 + eps^2, error-free up to the cross term
+    // R = |g|^2 + eps^2: squares error-free, cross terms 2 gh gl in FP32
     float s = __fmul_rn(gh[0], gh[0]);
     float lo = __fmaf_rn(gh[0], gh[0], -s);
     float c = __fmul_rn(gh[0], gl[0]);
 #pragma unroll
     for (int k = 1; k < DIM; k++) {
-        float p = __fmul_rn(gh[k], gh[k]);
-        float q = __fmaf_rn(gh[k], gh[k], -p);
-        float t = __fadd_rn(s, p);
+        const float p = __fmul_rn(gh[k], gh[k]);
+        const float q = __fmaf_rn(gh[k], gh[k], -p);
+        const float t = __fadd_rn(s, p);
         lo = __fadd_rn(lo, __fadd_rn(two_sum_err(s, p, t), q));
         s = t;
         c = __fmaf_rn(gh[k], gl[k], c);
     }
     {
-        float t = __fadd_rn(s, e2h);
-        lo = __fadd_rn(lo, __fadd_rn(two_sum_err(s, e2h, t), e2l));
+        const float t = __fadd_rn(s, e2h);
+        lo = __fadd_rn(lo, __fadd_rn(two_sum_err(s, e2h, t), __fmaf_rn(2.0f, c, e2l)));
         s = t;
     }
-    lo = __fadd_rn(lo, __fadd_rn(c, c));
     const float Rh = __fadd_rn(s, lo);
     const float Rl = __fsub_rn(lo, __fsub_rn(Rh, s));
-    if (!(Rh >= kTinyR && Rh <= kHugeR)) return false;
+    if (FAR) {
+        if (!(Rh >= kTinyR && Rh <= kHugeR)) return false;
+    } else {
+        if (!(Rh >= kTinyR)) return false;           // |dx| <= 2 inside the box
+    }
     // w = R^(-3/2): y ~ R^(-1/2); e = 1 - R y^2 exactly enough;
     // w = y^3 (1 - e)^(-3/2) = y^3 (1 + 3e/2 + 15e^2/8 + O(e^3))
     const float y = rsqrtf(Rh);
@@ -219,10 +233,10 @@ __device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4
     const float fl = __fmaf_rn(sh.w, wl, __fmaf_rn(sl.w, wh, __fmaf_rn(sh.w, wh, -fh)));
 #pragma unroll
     for (int k = 0; k < DIM; k++) {
-        float Fh = __fmul_rn(fh, gh[k]);
-        float Fl = __fmaf_rn(fh, gl[k], __fmaf_rn(fl, gh[k], __fmaf_rn(fh, gh[k], -Fh)));
-        float t = __fadd_rn(ah[k], Fh);
-        float err = two_sum_err(ah[k], Fh, t);
+        const float Fh = __fmul_rn(fh, gh[k]);
+        const float Fl = __fmaf_rn(fh, gl[k], __fmaf_rn(fl, gh[k], __fmaf_rn(fh, gh[k], -Fh)));
+        const float t = __fadd_rn(ah[k], Fh);
+        const float err = two_sum_err(ah[k], Fh, t);
         ah[k] = t;
         al[k] = __fadd_rn(al[k], __fadd_rn(err, Fl));
     }
@@ -287,11 +301,11 @@ struct FastArgs {
 
 template <int DIM, bool FAR>
 __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const FastArgs& a,
-                                     int w, int lane, bool valid, int32_t me, const float* Th,
+                                     int w, int lane, bool valid, int64_t me_sorted, const float* Th,
                                      const float* Tl, float band_abs, double x, double y, double z,
                                      float* ah, float* al, double* a64, int2 (*stack)[kStackDepth],
                                      float4 (*sh)[kWarp], float4 (*sl)[kWarp],
-                                     int32_t (*sid)[kWarp], unsigned long long* cnt, bool& overflow)
+                                     unsigned* cnt, bool& overflow)
 {
     const unsigned FULL = 0xffffffffu;
     const float theta_f = (float)a.theta;
@@ -307,8 +321,8 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
         const unsigned mask = (unsigned)e.y;
         const bool act = (mask >> lane) & 1u;
         cnt[2] += act;
-        const NodeCM cm = t.cm[node];
-        if (cm.w == 0.0) continue;                       // bh.py:514
+        // mass == 0 skip (bh.py:514), tested on the bits: +-0.0 only
+        if ((__double_as_longlong(__ldg(&t.cm[node].w)) << 1) == 0) continue;
         const int fc = t.first_child[node];
         if (fc < 0) {
             const int s = t.start[node], c = t.count[node];
@@ -317,20 +331,23 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                 if (jj < c) {
                     sh[w][lane] = ft.ph[s + jj];
                     sl[w][lane] = ft.pl[s + jj];
-                    sid[w][lane] = t.perm[s + jj];
                 }
                 __syncwarp();
                 const int cn = min(kWarp, c - b);
                 if (act) {
+                    // The target itself (self mode: sorted index `me_sorted`)
+                    // sits at zero displacement and adds exactly zero, so it
+                    // is not skipped; it is only left out of the pair count
+                    // (bh.py:254).
+                    cnt[0] += cn - (me_sorted >= s + b && me_sorted < s + b + cn);
+#pragma unroll 2
                     for (int q = 0; q < cn; q++) {
-                        if (sid[w][q] == me) continue;       // bh.py:254
                         if (!pair_ff<DIM, FAR>(Th, Tl, sh[w][q], sl[w][q], a.e2h, a.e2l, ah, al)) {
                             const int gi = s + b + q;
                             pair_fp64<DIM>(x, y, z, t.sx[gi], t.sy[gi], DIM == 3 ? t.sz[gi] : 0.0,
                                            t.sm[gi], eps2, a64);
                             cnt[4]++;
                         }
-                        cnt[0]++;
                     }
                 }
                 __syncwarp();
@@ -363,7 +380,7 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                 } else if (size_f < td - band) {
                     open = false;
                 } else {
-                    open = open_exact64<DIM>(x, y, z, cm, t.size[node], a.theta);
+                    open = open_exact64<DIM>(x, y, z, t.cm[node], t.size[node], a.theta);
                     cnt[3]++;
                 }
             }
@@ -371,6 +388,7 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
             if (act && !open) {
                 const float4 nl = ft.nl[node];
                 if (!pair_ff<DIM, FAR>(Th, Tl, nh, nl, a.e2h, a.e2l, ah, al)) {
+                    const NodeCM cm = t.cm[node];
                     pair_fp64<DIM>(x, y, z, cm.x, cm.y, cm.z, cm.w, eps2, a64);
                     cnt[4]++;
                 }
@@ -390,12 +408,11 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
 }
 
 template <int DIM>
-__global__ void __launch_bounds__(kFastThreads)
+__global__ void __launch_bounds__(kFastThreads, kFastBlocksPerSM)
 k_traverse_fast(TreeDev t, FastTree ft, FastArgs a)
 {
     __shared__ int2 stack[kFastWarps][kStackDepth];
     __shared__ float4 sh[kFastWarps][kWarp], sl[kFastWarps][kWarp];
-    __shared__ int32_t sid[kFastWarps][kWarp];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned FULL = 0xffffffffu;
     const FastFrame fr = *ft.frame;
@@ -409,7 +426,6 @@ k_traverse_fast(TreeDev t, FastTree ft, FastArgs a)
         bool far = false;
         float amax = 0.f;
         double x = 0.0, y = 0.0, z = 0.0;
-        int32_t me = -1;
         if (valid) {
             // self targets are the sorted particles themselves (inside the box)
             const float4 h = a.th ? a.th[i] : ft.ph[i];
@@ -421,23 +437,25 @@ k_traverse_fast(TreeDev t, FastTree ft, FastArgs a)
             x = a.tx[i];
             y = a.ty[i];
             z = DIM == 3 ? a.tz[i] : 0.0;
-            me = a.self_id ? a.self_id[i] : -1;
         }
         const float band_abs = kBandAbs * (1.0f + amax);
         float ah[3] = {0.f, 0.f, 0.f}, al[3] = {0.f, 0.f, 0.f};
         double a64[3] = {0.0, 0.0, 0.0};
-        unsigned long long cnt[5] = {0, 0, 0, 0, 0};
+        unsigned cnt[5] = {0, 0, 0, 0, 0};
+        // self mode: targets are the sorted particles, target i is particle i
+        const int64_t me_sorted = (valid && a.th == nullptr) ? i : -1;
         bool overflow = false;
         if (__any_sync(FULL, far))
-            walk<DIM, true>(t, ft, a, w, lane, valid, me, Th, Tl, band_abs, x, y, z, ah, al, a64,
-                            stack, sh, sl, sid, cnt, overflow);
+            walk<DIM, true>(t, ft, a, w, lane, valid, me_sorted, Th, Tl, band_abs, x, y, z, ah, al,
+                            a64, stack, sh, sl, cnt, overflow);
         else
-            walk<DIM, false>(t, ft, a, w, lane, valid, me, Th, Tl, band_abs, x, y, z, ah, al, a64,
-                             stack, sh, sl, sid, cnt, overflow);
+            walk<DIM, false>(t, ft, a, w, lane, valid, me_sorted, Th, Tl, band_abs, x, y, z, ah, al,
+                             a64, stack, sh, sl, cnt, overflow);
         if (overflow && lane == 0) atomicOr(a.err, kErrStackOverflow);
         if (a.stats) {
+#pragma unroll
             for (int k = 0; k < 5; k++) {
-                unsigned long long v = cnt[k];
+                unsigned long long v = cnt[k];   // per-target counts fit 32 bits
                 for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
                 if (lane == 0 && v) atomicAdd(&a.stats[k], v);
             }
