@@ -87,24 +87,44 @@ k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t 
         s_last = (ticket == gridDim.x - 1);
     }
     __syncthreads();
-    if (s_last && threadIdx.x == 0) {
-        __threadfence();
+    if (!s_last) return;
+    // last block: reduce all partials in parallel (strided over blocks)
+    __threadfence();
+    double a[7];
+    for (int d = 0; d < 3; d++) { a[d] = INFINITY; a[3 + d] = -INFINITY; }
+    a[6] = 0.0;
+    for (unsigned g = threadIdx.x; g < gridDim.x; g += blockDim.x) {
         for (int d = 0; d < 3; d++) {
-            double a = __ldcg(&partial[d]), b = __ldcg(&partial[3 + d]);
-            for (unsigned g = 1; g < gridDim.x; g++) {
-                double x = __ldcg(&partial[g * 8 + d]), y = __ldcg(&partial[g * 8 + 3 + d]);
-                a = x < a ? x : a;
-                b = y > b ? y : b;
+            double x = __ldcg(&partial[g * 8 + d]), y = __ldcg(&partial[g * 8 + 3 + d]);
+            a[d] = x < a[d] ? x : a[d];
+            a[3 + d] = y > a[3 + d] ? y : a[3 + d];
+        }
+        double mm = __ldcg(&partial[g * 8 + 6]);
+        a[6] = mm > a[6] ? mm : a[6];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int d = 0; d < 3; d++) {
+            double x = __shfl_down_sync(0xffffffffu, a[d], o);
+            double y = __shfl_down_sync(0xffffffffu, a[3 + d], o);
+            a[d] = x < a[d] ? x : a[d];
+            a[3 + d] = y > a[3 + d] ? y : a[3 + d];
+        }
+        double mm = __shfl_down_sync(0xffffffffu, a[6], o);
+        a[6] = mm > a[6] ? mm : a[6];
+    }
+    __shared__ double s_fin[kBoxThreads / 32][7];
+    if (lane == 0)
+        for (int k = 0; k < 7; k++) s_fin[warp][k] = a[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kBoxThreads / 32; w++) {
+            for (int d = 0; d < 3; d++) {
+                a[d] = s_fin[w][d] < a[d] ? s_fin[w][d] : a[d];
+                a[3 + d] = s_fin[w][3 + d] > a[3 + d] ? s_fin[w][3 + d] : a[3 + d];
             }
-            box[d] = a;
-            box[3 + d] = b;
+            a[6] = s_fin[w][6] > a[6] ? s_fin[w][6] : a[6];
         }
-        double mm = __ldcg(&partial[6]);
-        for (unsigned g = 1; g < gridDim.x; g++) {
-            double x = __ldcg(&partial[g * 8 + 6]);
-            mm = x > mm ? x : mm;
-        }
-        box[6] = mm;
+        for (int k = 0; k < 7; k++) box[k] = a[k];
         *done_counter = 0;
     }
 }
