@@ -25,6 +25,9 @@ FORM_EXACT = 0
 FORM_FAST = 1
 FORM_FP32 = 2
 FORMS = {"exact": FORM_EXACT, "fast": FORM_FAST, "fp32": FORM_FP32}
+MAC_BH = 0
+MAC_OFFSET = 1
+CRITERIA = {"bh": MAC_BH, "bh_offset": MAC_OFFSET}
 
 _VP = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -42,6 +45,7 @@ SIGNATURES = {
     "bhut_tree_accel_self": (_INT, [_VP, _D, _D, _D, _VP]),
     "bhut_tree_accel_targets": (_INT, [_VP, _VP, _I64, _D, _D, _D, _VP]),
     "bhut_tree_set_form": (_INT, [_VP, _INT]),
+    "bhut_tree_set_criterion": (_INT, [_VP, _INT]),
     "bhut_tree_info": (_INT, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                               ctypes.POINTER(_INT), ctypes.POINTER(_INT)]),
     "bhut_tree_export": (_INT, [_VP] * 11),

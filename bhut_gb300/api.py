@@ -10,7 +10,9 @@ and the result comes back as a CUDA tensor on the same device.
 One keyword is added to both entry points: ``form`` selects the traversal
 arithmetic -- ``"exact"`` (FP64; pair terms bit-identical to the reference's
 Numba loop), ``"fast"`` (FP64-accurate float-float arithmetic on the FP32
-pipe) or ``"fp32"`` (the FP32/Kahan precision form).
+pipe) or ``"fp32"`` (the FP32/Kahan precision form).  ``criterion`` accepts,
+besides the reference's ``"bh"``, ``"bh_offset"`` (open when
+|x - com| < size/theta + |com - box centre|), available with ``form="fp32"``.
 """
 from __future__ import annotations
 
@@ -159,6 +161,14 @@ def _form_code(form: str) -> int:
         raise ValueError(f"form must be one of {sorted(_lib.FORMS)}, got {form!r}") from None
 
 
+def _criterion_code(criterion: str, form: str) -> int:
+    if criterion not in _lib.CRITERIA:
+        raise ValueError(f"criterion must be 'bh', got '{criterion}'")
+    if criterion != "bh" and form != "fp32":
+        raise ValueError(f"criterion '{criterion}' is available with form='fp32' only")
+    return _lib.CRITERIA[criterion]
+
+
 # ---------------------------------------------------------------------------
 # TreeData export (bhut/tree/node.py:15-77)
 # ---------------------------------------------------------------------------
@@ -218,8 +228,9 @@ class _Handle:
         except Exception:
             pass
 
-    def set_form(self, form: str) -> None:
+    def set_form(self, form: str, criterion: str = "bh") -> None:
         _lib.check(self.L.bhut_tree_set_form(self.h, _form_code(form)))
+        _lib.check(self.L.bhut_tree_set_criterion(self.h, _criterion_code(criterion, form)))
 
     def build(self, pos, m) -> None:
         _sync_torch(pos, m)
@@ -311,10 +322,11 @@ def accelerations(
     monopole/P2P traversal at every particle, skipping self-interaction.
     Returns a float64 (N, dim) array (a CUDA tensor for CUDA tensor input).
     """
-    if criterion != "bh":
+    if criterion not in _lib.CRITERIA:
         raise ValueError(f"criterion must be 'bh', got '{criterion}'")
     if multipole != "mono":
         raise ValueError(f"multipole must be 'mono', got '{multipole}'")
+    _criterion_code(criterion, form or DEFAULT_FORM)
     _check_backend(positions, backend)
     positions, masses, softening = _validate_accelerations_inputs(
         positions, masses, dim=dim, softening=softening, theta=theta, G=G, leaf_size=leaf_size)
@@ -326,7 +338,7 @@ def accelerations(
         raise ValueError("Opening angle theta must be non-negative")
     h = _Handle(dim, leaf_size)
     try:
-        h.set_form(form or DEFAULT_FORM)
+        h.set_form(form or DEFAULT_FORM, criterion)
         h.build(positions, masses)
         out = _empty_like_out(positions, (n, dim))
         h.accel_self(theta, eps, G, out)
@@ -360,7 +372,7 @@ class Tree:
     """
 
     def __init__(self, positions, masses, *, leaf_size: int = 32, backend: str = "auto",
-                 dim: int = 3, form: str | None = None):
+                 dim: int = 3, form: str | None = None, criterion: str = "bh"):
         _validate_dimensions(dim)
         self.positions, self.masses, _ = _validate_accelerations_inputs(
             positions, masses, dim=dim, softening=0.0, theta=0.5, G=1.0, leaf_size=leaf_size)
@@ -372,6 +384,8 @@ class Tree:
         self._handle: _Handle | None = None
         self._form = form or DEFAULT_FORM
         _form_code(self._form)
+        self._criterion = criterion
+        _criterion_code(criterion, self._form)
         _check_backend(self.positions, backend)
 
     # -- reference attribute ``_tree``: None until built --------------------
@@ -399,9 +413,13 @@ class Tree:
         self._is_built = False
         self._tree_cache = None
 
-    def set_form(self, form: str) -> "Tree":
+    def set_form(self, form: str, criterion: str = "bh") -> "Tree":
+        """Traversal arithmetic ("exact", "fast", "fp32") and, for "fp32",
+        the opening criterion ("bh" or "bh_offset")."""
         _form_code(form)
+        _criterion_code(criterion, form)
         self._form = form
+        self._criterion = criterion
         return self
 
     def build(self) -> "Tree":
@@ -473,7 +491,7 @@ class Tree:
             raise ValueError(f"theta must be non-negative, got {theta}")
         out = _empty_like_out(targets, (M, self.dim))
         if M:
-            self._handle.set_form(self._form)
+            self._handle.set_form(self._form, self._criterion)
             self._handle.accel_targets(targets, theta, eps, G, out)
         return out
 
@@ -489,7 +507,7 @@ class Tree:
             raise ValueError("Opening angle theta must be non-negative")
         n = _shape(self.positions)[0]
         out = _empty_like_out(self.positions, (n, self.dim))
-        self._handle.set_form(self._form)
+        self._handle.set_form(self._form, self._criterion)
         self._handle.accel_self(theta, float(softening), G, out)
         return out
 

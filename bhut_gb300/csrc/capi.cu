@@ -112,8 +112,9 @@ struct bhut_tree {
     // traversal targets
     DevBuf tpos, tkeys, tperm, tx, ty, tz, tbox, out;
     // float-float copies for the fast form
-    DevBuf frame, ph, pl, nh, nl, nsize, th, tl;
+    DevBuf frame, ph, pl, nh, nl, nsize, ndelta, th, tl;
     bool ff_valid = false;
+    int mac = 0;
 
     TreeDev dev() const
     {
@@ -285,9 +286,11 @@ int prepare_fast(bhut_tree* t)
     BHUT_TRY(t->nh.ensure(sizeof(float4) * t->m, s));
     BHUT_TRY(t->nl.ensure(sizeof(float4) * t->m, s));
     BHUT_TRY(t->nsize.ensure(sizeof(float) * t->m, s));
+    BHUT_TRY(t->ndelta.ensure(sizeof(float) * t->m, s));
     BHUT_TRY(launch_fast_prepare(t->box.as<double>(), t->dim, t->frame.as<FastFrame>(), t->dev(),
-                                 t->ph.as<float4>(), t->pl.as<float4>(), t->nh.as<float4>(),
-                                 t->nl.as<float4>(), t->nsize.as<float>(), s));
+                                 t->center.as<double>(), t->ph.as<float4>(), t->pl.as<float4>(),
+                                 t->nh.as<float4>(), t->nl.as<float4>(), t->nsize.as<float>(),
+                                 t->ndelta.as<float>(), s));
     t->ff_valid = true;
     return kOk;
 }
@@ -295,7 +298,8 @@ int prepare_fast(bhut_tree* t)
 FastTree fast_tree(const bhut_tree* t)
 {
     return FastTree{t->frame.as<FastFrame>(), t->ph.as<float4>(), t->pl.as<float4>(),
-                    t->nh.as<float4>(), t->nl.as<float4>(), t->nsize.as<float>()};
+                    t->nh.as<float4>(), t->nl.as<float4>(), t->nsize.as<float>(),
+                    t->ndelta.as<float>()};
 }
 
 // Scale of the fast form's normalised coordinates (the frame's s), read
@@ -318,7 +322,8 @@ int traverse(bhut_tree* t, const double* tx, const double* ty, const double* tz,
     BHUT_CUDA(cudaMemsetAsync(t->stats.p, 0, sizeof(unsigned long long) * 8, t->stream));
     unsigned long long* st = t->stats.as<unsigned long long>();
     switch (t->form) {
-    case BHUT_FORM_FAST: {
+    case BHUT_FORM_FAST:
+    case BHUT_FORM_FP32: {
         BHUT_TRY(prepare_fast(t));
         double sc = 1.0;
         BHUT_TRY(frame_scale(t, &sc));
@@ -335,7 +340,8 @@ int traverse(bhut_tree* t, const double* tx, const double* ty, const double* tz,
         const double es = eps * sc;
         BHUT_TRY(launch_traverse_fast(d, fast_tree(t), th, tl, tx, ty, tz, self_id, out_idx, nt,
                                       theta, eps, G, es * es, out, t->err.as<unsigned>(), st,
-                                      t->stream));
+                                      t->stream, t->form == BHUT_FORM_FP32,
+                                      t->form == BHUT_FORM_FP32 ? t->mac : 0));
         break;
     }
     case BHUT_FORM_EXACT:
@@ -452,11 +458,22 @@ int bhut_tree_refit(bhut_tree* t, const double* positions, const double* masses,
 int bhut_tree_set_form(bhut_tree* t, int form)
 {
     if (!t) { set_error("tree is NULL"); return kInvalid; }
-    if (form != BHUT_FORM_EXACT && form != BHUT_FORM_FAST) {
+    if (form != BHUT_FORM_EXACT && form != BHUT_FORM_FAST && form != BHUT_FORM_FP32) {
         set_error("traversal form %d is not available in this build", form);
         return kInvalid;
     }
     t->form = form;
+    return kOk;
+}
+
+int bhut_tree_set_criterion(bhut_tree* t, int criterion)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (criterion != BHUT_MAC_BH && criterion != BHUT_MAC_OFFSET) {
+        set_error("unknown opening criterion %d", criterion);
+        return kInvalid;
+    }
+    t->mac = criterion;
     return kOk;
 }
 
@@ -588,7 +605,8 @@ void bhut_tree_destroy(bhut_tree* t)
                      &t->start, &t->count, &t->parent, &t->leaf_list, &t->arrive,
                      &t->sort_scratch, &t->box_partial, &t->box, &t->counters, &t->err, &t->stats,
                      &t->tpos, &t->tkeys, &t->tperm, &t->tx, &t->ty, &t->tz, &t->tbox, &t->out,
-                     &t->frame, &t->ph, &t->pl, &t->nh, &t->nl, &t->nsize, &t->th, &t->tl};
+                     &t->frame, &t->ph, &t->pl, &t->nh, &t->nl, &t->nsize, &t->ndelta, &t->th,
+                     &t->tl};
     for (DevBuf* b : all) b->release(s);
     cudaStreamSynchronize(s);
     if (t->own_stream) cudaStreamDestroy(s);
@@ -687,12 +705,16 @@ int bhut_direct_accelerations(const double* positions, const double* masses, int
     OutTarget o{nullptr, nullptr};
     size_t bytes = sizeof(double) * mt * dim;
     if (rc == kOk) rc = out_target(t, out, bytes, &o);
+    const int chunks = direct_chunks(n, mt);
+    DevBuf partial;
+    if (rc == kOk && chunks > 1) rc = partial.ensure(sizeof(double) * chunks * mt * dim, s);
     if (rc == kOk) rc = launch_direct(t->pos.as<double>(), t->mass.as<double>(), n, dim,
                                       targets ? t->tpos.as<double>() : nullptr,
                                       targets ? nullptr : self_idx.as<int64_t>(), mt, softening, G,
-                                      o.dev, s);
+                                      o.dev, partial.as<double>(), chunks, s);
     if (rc == kOk) rc = finish_out(t, o, bytes, "direct sum");
     self_idx.release(s);
+    partial.release(s);
     bhut_tree_destroy(t);
     return rc;
 }

@@ -179,14 +179,17 @@ k_traverse_exact(TreeDev t, const double* __restrict__ tx, const double* __restr
 
 // FP64 direct sum (the theta = 0 limit of the reference; pair arithmetic of
 // bh.py:262-278).  Targets given as AoS; self_id[i] >= 0 excludes that
-// source.  Sources are staged through shared memory in tiles.
+// source.  Sources are staged through shared memory in tiles.  Block
+// (x, y) handles targets [256x, 256x + 256) against source chunk y; with
+// more than one chunk, per-chunk partial sums go to `partial` and
+// k_direct_reduce adds them in chunk order (deterministic).
 constexpr int kDirectThreads = 256;
 
 template <int DIM>
 __global__ void __launch_bounds__(kDirectThreads)
 k_direct(const double* __restrict__ pos, const double* __restrict__ mass, int64_t n,
          const double* __restrict__ targets, const int64_t* __restrict__ self_id, int64_t nt,
-         double eps, double G, double* __restrict__ out)
+         double eps, double G, int64_t chunk, double* __restrict__ out)
 {
     __shared__ double sx[kDirectThreads], sy[kDirectThreads], sz[kDirectThreads],
         sm[kDirectThreads];
@@ -202,17 +205,19 @@ k_direct(const double* __restrict__ pos, const double* __restrict__ mass, int64_
     }
     const double eps2 = __dmul_rn(eps, eps);
     double ax = 0.0, ay = 0.0, az = 0.0;
-    for (int64_t b = 0; b < n; b += kDirectThreads) {
+    const int64_t j0 = (int64_t)blockIdx.y * chunk;
+    const int64_t j1 = j0 + chunk < n ? j0 + chunk : n;
+    for (int64_t b = j0; b < j1; b += kDirectThreads) {
         const int64_t j = b + threadIdx.x;
         __syncthreads();
-        if (j < n) {
+        if (j < j1) {
             sx[threadIdx.x] = pos[j * DIM];
             sy[threadIdx.x] = pos[j * DIM + 1];
             sz[threadIdx.x] = DIM == 3 ? pos[j * DIM + 2] : 0.0;
             sm[threadIdx.x] = mass[j];
         }
         __syncthreads();
-        const int cnt = (int)((n - b) < kDirectThreads ? (n - b) : kDirectThreads);
+        const int cnt = (int)((j1 - b) < kDirectThreads ? (j1 - b) : kDirectThreads);
         if (valid) {
             for (int q = 0; q < cnt; q++) {
                 if (b + q == me) continue;
@@ -232,9 +237,21 @@ k_direct(const double* __restrict__ pos, const double* __restrict__ mass, int64_
         }
     }
     if (valid) {
-        out[i * DIM] = ax;
-        out[i * DIM + 1] = ay;
-        if (DIM == 3) out[i * DIM + 2] = az;
+        double* o = out + ((int64_t)blockIdx.y * nt + i) * DIM;
+        o[0] = ax;
+        o[1] = ay;
+        if (DIM == 3) o[2] = az;
+    }
+}
+
+__global__ void k_direct_reduce(const double* __restrict__ partial, int64_t nt, int dim,
+                                int chunks, double* __restrict__ out)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nt * dim;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        double s = partial[k];
+        for (int c = 1; c < chunks; c++) s = __dadd_rn(s, partial[(int64_t)c * nt * dim + k]);
+        out[k] = s;
     }
 }
 
@@ -257,18 +274,33 @@ int launch_traverse_exact(const TreeDev& t, const double* tx, const double* ty, 
     return kOk;
 }
 
+int direct_chunks(int64_t n, int64_t nt)
+{
+    const int64_t tblocks = (nt + kDirectThreads - 1) / kDirectThreads;
+    int64_t want = (152 * 8 + tblocks - 1) / tblocks;        // fill the GPU ~8 blocks per SM
+    int64_t maxc = (n + 4095) / 4096;                         // at least 4096 sources a chunk
+    int64_t c = want < maxc ? want : maxc;
+    return (int)(c < 1 ? 1 : (c > 1024 ? 1024 : c));
+}
+
 int launch_direct(const double* pos, const double* mass, int64_t n, int dim, const double* targets,
                   const int64_t* self_id, int64_t nt, double eps, double G, double* out,
-                  cudaStream_t s)
+                  double* partial, int chunks, cudaStream_t s)
 {
     if (nt <= 0) return kOk;
-    unsigned grid = (unsigned)((nt + kDirectThreads - 1) / kDirectThreads);
+    const int64_t chunk = (n + chunks - 1) / chunks;
+    dim3 grid((unsigned)((nt + kDirectThreads - 1) / kDirectThreads), (unsigned)chunks);
+    double* dst = chunks > 1 ? partial : out;
     if (dim == 3)
-        k_direct<3><<<grid, kDirectThreads, 0, s>>>(pos, mass, n, targets, self_id, nt, eps, G, out);
+        k_direct<3><<<grid, kDirectThreads, 0, s>>>(pos, mass, n, targets, self_id, nt, eps, G, chunk,
+                                                    dst);
     else
-        k_direct<2><<<grid, kDirectThreads, 0, s>>>(pos, mass, n, targets, self_id, nt, eps, G, out);
+        k_direct<2><<<grid, kDirectThreads, 0, s>>>(pos, mass, n, targets, self_id, nt, eps, G, chunk,
+                                                    dst);
+    if (chunks > 1)
+        k_direct_reduce<<<grid_for(nt * dim, 256), 256, 0, s>>>(partial, nt, dim, chunks, out);
     BHUT_CUDA(cudaGetLastError());
-    note_launches(1);
+    note_launches(chunks > 1 ? 2 : 1);
     return kOk;
 }
 

@@ -19,9 +19,11 @@
 //    computed exactly (Newton-Raphson for the inverse square root, carried
 //    to second order); m * w * dx and the accumulation are float-float
 //    (Dekker/Knuth two-product and TwoSum).
-//  * Pairs closer than 2^-15 in normalised units (2^-14 of the box
-//    half-size), or outside the FP32 range, are evaluated in FP64 from the
-//    FP64 arrays instead.
+//  * Pairs with r^2 + eps^2 below 2^-34 in normalised units (softened
+//    distance under 2^-16 of the box half-size), or outside the FP32 range,
+//    are evaluated in FP64 from the FP64 arrays instead; above it a pair's
+//    relative error, dominated by the 2^-48 coordinate representation, stays
+//    below 2^-30.
 //  * The opening decision is the reference's, bit for bit: a FP32 test
 //    decides every node whose ratio is clearly above or below theta, and
 //    nodes inside a small error band are decided by the exact FP64 test of
@@ -34,10 +36,13 @@ namespace bhut {
 constexpr int kFastWarps = 4;
 constexpr int kFastThreads = kFastWarps * kWarp;
 constexpr int kFastBlocksPerSM = 6;    // 24 warps per SM: registers capped at 80
-constexpr float kTinyR = 0x1p-30f;     // r^2 below this (normalised) -> FP64 pair
+// r^2 + eps^2 below this (normalised units) -> FP64 pair.  The coordinates
+// are represented to 2^-48, so a pair's relative error is about
+// 2^-47 / sqrt(R): at most 2^-30 on the fast path.
+constexpr float kTinyR = 0x1p-34f;
 constexpr float kHugeR = 0x1p+100f;    // r^2 above this -> FP64 pair
 constexpr float kBandRel = 0x1p-18f;   // opening-test error band, relative part
-constexpr float kBandAbs = 0x1p-21f;   // ... absolute part per unit of (1 + |target|)
+constexpr float kBandAbs = 0x1p-40f;   // ... absolute part per unit of (1 + |target|)
 
 // ---------------------------------------------------------------------------
 // frame (normalisation) derived from the tree's bounding box
@@ -108,9 +113,10 @@ __global__ void k_ff_particles(const double* __restrict__ sx, const double* __re
 }
 
 __global__ void k_ff_nodes(const NodeCM* __restrict__ cm, const double* __restrict__ size,
-                           int64_t m, int dim, const FastFrame* __restrict__ fr,
-                           float4* __restrict__ nh, float4* __restrict__ nl,
-                           float* __restrict__ nsize)
+                           const double* __restrict__ center, int64_t m, int dim,
+                           const FastFrame* __restrict__ fr, float4* __restrict__ nh,
+                           float4* __restrict__ nl, float* __restrict__ nsize,
+                           float* __restrict__ ndelta)
 {
     const FastFrame f = *fr;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m;
@@ -126,6 +132,14 @@ __global__ void k_ff_nodes(const NodeCM* __restrict__ cm, const double* __restri
         nh[k] = h;
         nl[k] = l;
         nsize[k] = __double2float_rn(__dmul_rn(size[k], f.s));
+        // distance between the centre of mass and the AABB centre (offset MAC)
+        double dd = 0.0;
+        for (int d = 0; d < dim; d++) {
+            const double cc = d == 0 ? c.x : (d == 1 ? c.y : c.z);
+            const double v = cc - center[k * dim + d];
+            dd += v * v;
+        }
+        ndelta[k] = __double2float_ru(sqrt(dd) * f.s);
     }
 }
 
@@ -297,6 +311,7 @@ struct FastArgs {
     double* out;
     unsigned* err;
     unsigned long long* stats;
+    int mac;                 // 0: reference criterion, 1: offset criterion (fp32 form)
 };
 
 template <int DIM, bool FAR>
@@ -365,10 +380,12 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
             float4 nh = make_float4(0.f, 0.f, 0.f, 0.f);
             if (act) {
                 nh = ft.nh[node];
+                const float4 nlo = ft.nl[node];
                 float d2 = 0.0f;
 #pragma unroll
                 for (int k = 0; k < DIM; k++) {
-                    float d = comp(nh, k) - Th[k];
+                    // hi and lo differences (both exact inside the box), rounded once
+                    float d = __fadd_rn(__fsub_rn(comp(nh, k), Th[k]), __fsub_rn(comp(nlo, k), Tl[k]));
                     d2 = fmaf(d, d, d2);
                 }
                 const float dist = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
@@ -386,7 +403,7 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
             }
             const unsigned omask = __ballot_sync(FULL, act && open);
             if (act && !open) {
-                const float4 nl = ft.nl[node];
+                const float4 nl = ft.nl[node];   // (cached: read by the opening test)
                 if (!pair_ff<DIM, FAR>(Th, Tl, nh, nl, a.e2h, a.e2l, ah, al)) {
                     const NodeCM cm = t.cm[node];
                     pair_fp64<DIM>(x, y, z, cm.x, cm.y, cm.z, cm.w, eps2, a64);
@@ -472,16 +489,171 @@ k_traverse_fast(TreeDev t, FastTree ft, FastArgs a)
 }
 
 // ---------------------------------------------------------------------------
+// form "fp32": the precision form.  Pair terms, monopoles and the opening
+// test in FP32 on the grid-aligned hi coordinates; per-target sums with
+// Kahan compensation.  FP64 stays in the tree build (bounding box, Morton
+// keys, masses and centres of mass) and in the final scaling.
+// ---------------------------------------------------------------------------
+// Displacement from the hi parts (exact on the grid) plus the lo parts
+// (exact on their grid), rounded once: FP32-relative accuracy everywhere in
+// the box, also in dense regions far from the box centre.
+template <int DIM>
+__device__ __forceinline__ void pair_f32(const float* Th, const float* Tl, float4 sh, float4 sl,
+                                         float e2, float* acc, float* cmp)
+{
+    const float d0 = __fadd_rn(__fsub_rn(sh.x, Th[0]), __fsub_rn(sl.x, Tl[0]));
+    const float d1 = __fadd_rn(__fsub_rn(sh.y, Th[1]), __fsub_rn(sl.y, Tl[1]));
+    const float d2 = DIM == 3 ? __fadd_rn(__fsub_rn(sh.z, Th[2]), __fsub_rn(sl.z, Tl[2])) : 0.0f;
+    float r2 = fmaf(d1, d1, fmaf(d0, d0, e2));
+    if (DIM == 3) r2 = fmaf(d2, d2, r2);
+    if (!(r2 > 0.0f)) return;                  // r^2 + eps^2 == 0: no term (kernels.py:62-63)
+    const float ri = rsqrtf(r2);
+    const float f = sh.w * (ri * ri * ri);
+    const float d[3] = {d0, d1, d2};
+#pragma unroll
+    for (int k = 0; k < DIM; k++) {            // Kahan compensated sum
+        const float y = __fsub_rn(__fmul_rn(f, d[k]), cmp[k]);
+        const float t = __fadd_rn(acc[k], y);
+        cmp[k] = __fsub_rn(__fsub_rn(t, acc[k]), y);
+        acc[k] = t;
+    }
+}
+
+template <int DIM>
+__device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, const FastArgs& a,
+                                         int w, int lane, bool valid, int64_t me_sorted,
+                                         const float* T, const float* Tl, float* acc, float* cmp,
+                                         int2 (*stack)[kStackDepth], float4 (*sh)[kWarp],
+                                         float4 (*sl)[kWarp], unsigned* cnt, bool& overflow)
+{
+    const unsigned FULL = 0xffffffffu;
+    const float theta_f = (float)a.theta;
+    const unsigned live = __ballot_sync(FULL, valid);
+    if (lane == 0) stack[w][0] = make_int2(0, (int)live);
+    int sp = 1;
+    __syncwarp();
+    while (sp > 0) {
+        const int2 e = stack[w][--sp];
+        __syncwarp();
+        const int node = e.x;
+        const unsigned mask = (unsigned)e.y;
+        const bool act = (mask >> lane) & 1u;
+        cnt[2] += act;
+        if ((__double_as_longlong(__ldg(&t.cm[node].w)) << 1) == 0) continue;
+        const int fc = t.first_child[node];
+        if (fc < 0) {
+            const int s = t.start[node], c = t.count[node];
+            for (int b = 0; b < c; b += kWarp) {
+                const int jj = b + lane;
+                if (jj < c) {
+                    sh[w][lane] = ft.ph[s + jj];
+                    sl[w][lane] = ft.pl[s + jj];
+                }
+                __syncwarp();
+                const int cn = min(kWarp, c - b);
+                if (act) {
+                    cnt[0] += cn - (me_sorted >= s + b && me_sorted < s + b + cn);
+#pragma unroll 4
+                    for (int q = 0; q < cn; q++)
+                        pair_f32<DIM>(T, Tl, sh[w][q], sl[w][q], a.e2h, acc, cmp);
+                }
+                __syncwarp();
+            }
+        } else {
+            bool open = false;
+            float4 nh = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (act) {
+                nh = ft.nh[node];
+                const float4 nlo = ft.nl[node];
+                float d2 = 0.0f;
+#pragma unroll
+                for (int k = 0; k < DIM; k++) {
+                    const float d = __fadd_rn(__fsub_rn(comp(nh, k), T[k]),
+                                              __fsub_rn(comp(nlo, k), Tl[k]));
+                    d2 = fmaf(d, d, d2);
+                }
+                const float dist = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+                const float size_f = ft.nsize[node];
+                if (a.mac == 1) {
+                    // offset criterion: open when d < size/theta + |com - centre|
+                    open = size_f >= theta_f * (dist - ft.ndelta[node]);
+                } else {
+                    open = dist == 0.0f || size_f >= theta_f * dist;
+                }
+            }
+            const unsigned omask = __ballot_sync(FULL, act && open);
+            if (act && !open) {
+                pair_f32<DIM>(T, Tl, nh, ft.nl[node], a.e2h, acc, cmp);
+                cnt[1]++;
+            }
+            if (omask) {
+                if (sp + 2 > kStackDepth) { overflow = true; break; }
+                if (lane == 0) {
+                    stack[w][sp] = make_int2(fc, (int)omask);
+                    stack[w][sp + 1] = make_int2(fc + 1, (int)omask);
+                }
+                sp += 2;
+                __syncwarp();
+            }
+        }
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kFastThreads)
+k_traverse_fp32(TreeDev t, FastTree ft, FastArgs a)
+{
+    __shared__ int2 stack[kFastWarps][kStackDepth];
+    __shared__ float4 sh[kFastWarps][kWarp], sl[kFastWarps][kWarp];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned FULL = 0xffffffffu;
+    const double conv = __dmul_rn(ft.frame->conv, a.G);
+    for (int64_t base = ((int64_t)blockIdx.x * kFastWarps + w) * kWarp; base < a.nt;
+         base += (int64_t)gridDim.x * kFastWarps * kWarp) {
+        const int64_t i = base + lane;
+        const bool valid = i < a.nt;
+        float T[3] = {0.f, 0.f, 0.f}, Tl[3] = {0.f, 0.f, 0.f};
+        if (valid) {
+            const float4 h = a.th ? a.th[i] : ft.ph[i];
+            const float4 l = a.th ? a.tl[i] : ft.pl[i];
+            T[0] = h.x; T[1] = h.y; T[2] = h.z;
+            Tl[0] = l.x; Tl[1] = l.y; Tl[2] = l.z;
+        }
+        float acc[3] = {0.f, 0.f, 0.f}, cmp[3] = {0.f, 0.f, 0.f};
+        unsigned cnt[5] = {0, 0, 0, 0, 0};
+        const int64_t me_sorted = (valid && a.th == nullptr) ? i : -1;
+        bool overflow = false;
+        walk_f32<DIM>(t, ft, a, w, lane, valid, me_sorted, T, Tl, acc, cmp, stack, sh, sl, cnt,
+                      overflow);
+        if (overflow && lane == 0) atomicOr(a.err, kErrStackOverflow);
+        if (a.stats) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                unsigned long long v = cnt[k];
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+                if (lane == 0 && v) atomicAdd(&a.stats[k], v);
+            }
+        }
+        if (valid) {
+            const int64_t o = a.out_idx ? a.out_idx[i] : i;
+#pragma unroll
+            for (int k = 0; k < DIM; k++) a.out[o * DIM + k] = __dmul_rn((double)acc[k], conv);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 int launch_fast_prepare(const double* box, int dim, FastFrame* frame, const TreeDev& t,
-                        float4* ph, float4* pl, float4* nh, float4* nl, float* nsize,
-                        cudaStream_t s)
+                        const double* center, float4* ph, float4* pl, float4* nh, float4* nl,
+                        float* nsize, float* ndelta, cudaStream_t s)
 {
     k_frame<<<1, 32, 0, s>>>(box, dim, frame);
     k_ff_particles<<<grid_for(t.n, 256), 256, 0, s>>>(t.sx, t.sy, t.sz, t.sm, t.n, dim, frame, ph,
                                                       pl);
-    k_ff_nodes<<<grid_for(t.m, 256), 256, 0, s>>>(t.cm, t.size, t.m, dim, frame, nh, nl, nsize);
+    k_ff_nodes<<<grid_for(t.m, 256), 256, 0, s>>>(t.cm, t.size, center, t.m, dim, frame, nh, nl,
+                                                  nsize, ndelta);
     BHUT_CUDA(cudaGetLastError());
     note_launches(3);
     return kOk;
@@ -500,7 +672,7 @@ int launch_traverse_fast(const TreeDev& t, const FastTree& ft, const float4* th,
                          const double* tx, const double* ty, const double* tz,
                          const int32_t* self_id, const int32_t* out_idx, int64_t nt, double theta,
                          double eps, double G, double eps_scaled_sq, double* out, unsigned* err,
-                         unsigned long long* stats, cudaStream_t s)
+                         unsigned long long* stats, cudaStream_t s, bool fp32, int mac)
 {
     if (nt <= 0) return kOk;
     FastArgs a;
@@ -509,11 +681,17 @@ int launch_traverse_fast(const TreeDev& t, const FastTree& ft, const float4* th,
     a.theta = theta; a.eps = eps; a.G = G;
     a.e2h = (float)eps_scaled_sq;
     a.e2l = (float)(eps_scaled_sq - (double)a.e2h);
-    a.out = out; a.err = err; a.stats = stats;
+    a.out = out; a.err = err; a.stats = stats; a.mac = mac;
     int64_t warps = (nt + kWarp - 1) / kWarp;
     unsigned grid = grid_for(warps, kFastWarps, 152u * 64u);
-    if (t.dim == 3) k_traverse_fast<3><<<grid, kFastThreads, 0, s>>>(t, ft, a);
-    else k_traverse_fast<2><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+    if (fp32) {
+        if (t.dim == 3) k_traverse_fp32<3><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+        else k_traverse_fp32<2><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+    } else if (t.dim == 3) {
+        k_traverse_fast<3><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+    } else {
+        k_traverse_fast<2><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+    }
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
     return kOk;

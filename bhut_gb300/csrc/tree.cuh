@@ -66,6 +66,7 @@ struct FastTree {
     const float4* nh;   // (com, mass) hi per node
     const float4* nl;   // (com, mass) lo per node
     const float* nsize; // 2 * half_size, normalised, per node
+    const float* ndelta; // |com - AABB centre|, normalised, per node (offset criterion)
 };
 
 // Node arrays written by the bottom-up pass.
@@ -104,17 +105,18 @@ int launch_traverse_exact(const TreeDev& t, const double* tx, const double* ty, 
                           double eps, double G, double* out, unsigned* err,
                           unsigned long long* stats, cudaStream_t s);
 int launch_fast_prepare(const double* box, int dim, FastFrame* frame, const TreeDev& t,
-                        float4* ph, float4* pl, float4* nh, float4* nl, float* nsize,
-                        cudaStream_t s);
+                        const double* center, float4* ph, float4* pl, float4* nh, float4* nl,
+                        float* nsize, float* ndelta, cudaStream_t s);
 int launch_fast_targets(const double* tx, const double* ty, const double* tz, int64_t nt, int dim,
                         const FastFrame* frame, float4* th, float4* tl, cudaStream_t s);
 int launch_traverse_fast(const TreeDev& t, const FastTree& ft, const float4* th, const float4* tl,
                          const double* tx, const double* ty, const double* tz,
                          const int32_t* self_id, const int32_t* out_idx, int64_t nt, double theta,
                          double eps, double G, double eps_scaled_sq, double* out, unsigned* err,
-                         unsigned long long* stats, cudaStream_t s);
+                         unsigned long long* stats, cudaStream_t s, bool fp32, int mac);
+int direct_chunks(int64_t n, int64_t nt);
 int launch_direct(const double* pos, const double* mass, int64_t n, int dim, const double* targets,
                   const int64_t* self_id, int64_t nt, double eps, double G, double* out,
-                  cudaStream_t s);
+                  double* partial, int chunks, cudaStream_t s);
 
 }  // namespace bhut

@@ -44,6 +44,10 @@ extern "C" {
 #define BHUT_FORM_FAST 1   /* FP64-accurate float-float on the FP32 pipe (default) */
 #define BHUT_FORM_FP32 2   /* precision form: FP32 with Kahan-compensated sums */
 
+/* Opening criteria (bhut_tree_set_criterion). */
+#define BHUT_MAC_BH 0      /* 2 h / |x - com| >= theta -> open (bhut/traverse/bh.py:576-601) */
+#define BHUT_MAC_OFFSET 1  /* open when |x - com| < 2 h / theta + |com - AABB centre| */
+
 typedef struct bhut_tree bhut_tree;
 
 /* Library version string. */
@@ -102,6 +106,11 @@ BHUT_API int bhut_tree_fallbacks(const bhut_tree *t, int64_t *exact_decisions, i
 
 /* Total number of kernels this library has launched in the process. */
 BHUT_API long long bhut_launch_count(void);
+
+/* Opening criterion of the FP32 form (BHUT_MAC_*; default BHUT_MAC_BH).  The
+ * exact and fast forms always use the reference criterion.  No counterpart
+ * in the reference, whose only criterion is "bh" (bhut/api.py:306-307). */
+BHUT_API int bhut_tree_set_criterion(bhut_tree *t, int criterion);
 
 /* n, node count, dim, leaf size of a built tree. */
 BHUT_API int bhut_tree_info(const bhut_tree *t, int64_t *n, int64_t *num_nodes, int *dim, int *leaf_size);

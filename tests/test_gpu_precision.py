@@ -1,0 +1,74 @@
+"""The FP32 precision form (FP32 traversal/P2P, Kahan-compensated sums) and
+the offset opening criterion, on the GPU."""
+import numpy as np
+import pytest
+
+import bhut_gb300 as bh
+from bhut_gb300 import precision, workloads
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _engine(engine_lib):
+    yield
+
+
+@pytest.fixture(scope="module")
+def plummer200k():
+    return workloads.plummer(200_000, seed=31)
+
+
+def test_fp32_close_to_fp64_plain(plummer200k):
+    pos, m = plummer200k
+    t64 = bh.Tree(pos, m, form="fast").build()
+    a64 = t64.accelerations(theta=0.5, softening=0.01)
+    n64 = t64._handle.stats()
+    t32 = bh.Tree(pos, m, form="fp32").build()
+    a32 = t32.accelerations(theta=0.5, softening=0.01)
+    n32 = t32._handle.stats()
+    dist = precision.error_distribution(a32, a64)
+    # FP32 arithmetic: ~1e-6 per target; an opening decision that flips at the
+    # FP32/FP64 margin changes that target by the MAC error (~1e-3), rarely
+    assert dist["median"] < 2e-6, dist
+    assert dist["rel_l2"] < 1e-4, dist
+    # the same interaction set up to decisions at the margin
+    assert abs(n32[0] - n64[0]) <= 1e-4 * n64[0]
+    assert abs(n32[1] - n64[1]) <= 1e-3 * n64[1]
+    t64.close()
+    t32.close()
+
+
+def test_fp32_external_targets_and_2d():
+    pos, m = workloads.gaussian(20_000, seed=3)
+    tg = workloads.cube_targets(3000, seed=4, side=12.0)
+    a = bh.Tree(pos, m, form="fp32").build().accelerations(tg, theta=0.6, softening=0.02)
+    b = bh.Tree(pos, m, form="fast").build().accelerations(tg, theta=0.6, softening=0.02)
+    assert rel_l2(a, b) < 1e-4
+    pos2, m2 = workloads.gaussian(5000, seed=5, dim=2)
+    a = bh.accelerations(pos2, m2, dim=2, form="fp32", theta=0.5, softening=0.02)
+    b = bh.accelerations(pos2, m2, dim=2, form="fast", theta=0.5, softening=0.02)
+    assert rel_l2(a, b) < 1e-4
+
+
+def test_offset_criterion_is_more_accurate(plummer200k):
+    pos, m = plummer200k
+    idx = precision.sample_indices(len(pos), 1024, seed=2)
+    ref = precision.direct_reference(pos, m, idx, softening=0.01)
+    e_bh = precision.error_distribution(
+        bh.accelerations(pos, m, form="fp32", theta=0.5, softening=0.01)[idx], ref)
+    e_off = precision.error_distribution(
+        bh.accelerations(pos, m, form="fp32", criterion="bh_offset", theta=0.5,
+                         softening=0.01)[idx], ref)
+    assert e_off["median"] < e_bh["median"]
+    with pytest.raises(ValueError, match="form='fp32'"):
+        bh.accelerations(pos[:10], m[:10], criterion="bh_offset", form="fast")
+
+
+def test_direct_reference_matches_theta_zero():
+    pos, m = workloads.plummer(4000, seed=8)
+    idx = precision.sample_indices(len(pos), 256, seed=1)
+    ref = precision.direct_reference(pos, m, idx, softening=0.01)
+    a0 = bh.accelerations(pos, m, theta=0.0, softening=0.01, form="exact")
+    assert rel_l2(a0[idx], ref) < 1e-13
