@@ -29,68 +29,20 @@
 //    nodes inside a small error band are decided by the exact FP64 test of
 //    k_traverse_exact (bh.py:576-601).  Every lane therefore evaluates
 //    exactly the reference's interaction set for its target.
-#include "tree.cuh"
+#include "fast.cuh"
 
 namespace bhut {
 
 constexpr int kFastWarps = 4;
 constexpr int kFastThreads = kFastWarps * kWarp;
 constexpr int kFastBlocksPerSM = 6;    // 24 warps per SM: registers capped at 80
-// r^2 + eps^2 below this (normalised units) -> FP64 pair.  The coordinates
-// are represented to 2^-48, so a pair's relative error is about
-// 2^-47 / sqrt(R): at most 2^-30 on the fast path.
-constexpr float kTinyR = 0x1p-34f;
-constexpr float kHugeR = 0x1p+100f;    // r^2 above this -> FP64 pair
-constexpr float kBandRel = 0x1p-18f;   // opening-test error band, relative part
-constexpr float kBandAbs = 0x1p-40f;   // ... absolute part per unit of (1 + |target|)
 
 // ---------------------------------------------------------------------------
 // frame (normalisation) derived from the tree's bounding box
 // ---------------------------------------------------------------------------
-__device__ void frame_from_box(const double* box, int dim, FastFrame* f)
-{
-    double h = 0.0;
-    for (int d = 0; d < 3; d++) f->c[d] = 0.0;
-    for (int d = 0; d < dim; d++) {
-        f->c[d] = __dmul_rn(__dadd_rn(box[d], box[3 + d]), 0.5);
-        double e = __dmul_rn(__dsub_rn(box[3 + d], box[d]), 0.5);
-        h = e > h ? e : h;
-    }
-    if (!(h > 0.0)) h = 1.0;
-    // Map the box into [-1/2, 1/2]: a refit may move particles to 1.1x the
-    // root box (bhut/tree/refit.py:236-249) and targets inside [-1, 1] are
-    // still on the grid; every hi difference then stays below 2 and is exact.
-    int ex;
-    frexp(h, &ex);                      // h <= 2^ex
-    f->s = ldexp(1.0, -ex - 1);
-    double mm = box[6];
-    int em = 0;
-    if (mm > 0.0) frexp(mm, &em);       // |m| <= 2^em
-    f->ms = ldexp(1.0, -em);
-    f->conv = ldexp(1.0, em - 2 * ex - 2);  // normalised -> physical acceleration (s^2 / ms)
-}
-
 __global__ void k_frame(const double* __restrict__ box, int dim, FastFrame* __restrict__ f)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) frame_from_box(box, dim, f);
-}
-
-// hi on the 2^-23 grid and lo on the 2^-47 grid (both exact in FP32 for
-// |u| <= 1): differences of hi parts, and of lo parts, are then exact in
-// FP32; u is represented to within 2^-48.
-__device__ __forceinline__ void split_grid(double u, float& h, float& l)
-{
-    double H = rint(__dmul_rn(u, 8388608.0));
-    double hd = __dmul_rn(H, 1.0 / 8388608.0);
-    h = __double2float_rn(hd);
-    double L = rint(__dmul_rn(__dsub_rn(u, hd), 140737488355328.0));   // 2^47
-    l = __double2float_rn(__dmul_rn(L, 1.0 / 140737488355328.0));
-}
-
-__device__ __forceinline__ void split_plain(double u, float& h, float& l)
-{
-    h = __double2float_rn(u);
-    l = __double2float_rn(__dsub_rn(u, (double)h));
 }
 
 __global__ void k_ff_particles(const double* __restrict__ sx, const double* __restrict__ sy,
@@ -166,132 +118,6 @@ __global__ void k_ff_targets(const double* __restrict__ tx, const double* __rest
         th[i] = make_float4(hh[0], hh[1], hh[2], inside ? 0.0f : 1.0f);
         tl[i] = make_float4(ll[0], ll[1], ll[2], __double2float_ru(amax));
     }
-}
-
-// ---------------------------------------------------------------------------
-// float-float pair term
-// ---------------------------------------------------------------------------
-// Error of s = fl(a + b) (Knuth's TwoSum).
-__device__ __forceinline__ float two_sum_err(float a, float b, float s)
-{
-    float bb = __fsub_rn(s, a);
-    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-__device__ __forceinline__ float comp(const float4& v, int k)
-{
-    return k == 0 ? v.x : (k == 1 ? v.y : v.z);
-}
-
-// Adds G-less m * (x_src - x_tgt) / (|dx|^2 + eps^2)^(3/2), normalised
-// units, to (ah, al).  Returns false when the pair must go to FP64.
-//
-// d = hi_src - hi_tgt is exact on the grid and l = lo_src - lo_tgt is small
-// (|l| <= 2^-23), so (d, l) is renormalised with FastTwoSum into (gh, gl),
-// |gl| <= ulp(gh) / 2; every later product of a float-float with g then
-// keeps ~2^-47 relative accuracy.  A pair at zero displacement (the target
-// itself, or a duplicate) contributes exactly zero, as in the reference.
-template <int DIM, bool FAR>
-__device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4 sh, float4 sl,
-                                        float e2h, float e2l, float* ah, float* al)
-{
-    float gh[3], gl[3];
-#pragma unroll
-    for (int k = 0; k < DIM; k++) {
-        const float xh = comp(sh, k);
-        const float d = __fsub_rn(xh, Th[k]);        // exact on the grid
-        float l = __fsub_rn(comp(sl, k), Tl[k]);
-        if (FAR) l = __fadd_rn(l, two_sum_err(xh, -Th[k], d));
-        const float h = __fadd_rn(d, l);             // FastTwoSum(d, l), |l| <= |d| or d == 0
-        gl[k] = __fsub_rn(l, __fsub_rn(h, d));
-        gh[k] = h;
-    }
-    // R = |g|^2 + eps^2: squares error-free, cross terms 2 gh gl in FP32
-    float s = __fmul_rn(gh[0], gh[0]);
-    float lo = __fmaf_rn(gh[0], gh[0], -s);
-    float c = __fmul_rn(gh[0], gl[0]);
-#pragma unroll
-    for (int k = 1; k < DIM; k++) {
-        const float p = __fmul_rn(gh[k], gh[k]);
-        const float q = __fmaf_rn(gh[k], gh[k], -p);
-        const float t = __fadd_rn(s, p);
-        lo = __fadd_rn(lo, __fadd_rn(two_sum_err(s, p, t), q));
-        s = t;
-        c = __fmaf_rn(gh[k], gl[k], c);
-    }
-    {
-        const float t = __fadd_rn(s, e2h);
-        lo = __fadd_rn(lo, __fadd_rn(two_sum_err(s, e2h, t), __fmaf_rn(2.0f, c, e2l)));
-        s = t;
-    }
-    const float Rh = __fadd_rn(s, lo);
-    const float Rl = __fsub_rn(lo, __fsub_rn(Rh, s));
-    if (FAR) {
-        if (!(Rh >= kTinyR && Rh <= kHugeR)) return false;
-    } else {
-        if (!(Rh >= kTinyR)) return false;           // |dx| <= 2 inside the box
-    }
-    // w = R^(-3/2): y ~ R^(-1/2); e = 1 - R y^2 exactly enough;
-    // w = y^3 (1 - e)^(-3/2) = y^3 (1 + 3e/2 + 15e^2/8 + O(e^3))
-    const float y = rsqrtf(Rh);
-    const float Y = __fmul_rn(y, y);
-    const float Ye = __fmaf_rn(y, y, -Y);
-    const float e = -__fmaf_rn(Rh, Ye, __fmaf_rn(Rl, Y, __fmaf_rn(Rh, Y, -1.0f)));
-    const float W = __fmul_rn(Y, y);
-    const float We = __fmaf_rn(Ye, y, __fmaf_rn(Y, y, -W));
-    const float corr = __fmul_rn(e, __fmaf_rn(1.875f, e, 1.5f));
-    const float wh = W;
-    const float wl = __fmaf_rn(W, corr, We);
-    // f = m w
-    const float fh = __fmul_rn(sh.w, wh);
-    const float fl = __fmaf_rn(sh.w, wl, __fmaf_rn(sl.w, wh, __fmaf_rn(sh.w, wh, -fh)));
-#pragma unroll
-    for (int k = 0; k < DIM; k++) {
-        const float Fh = __fmul_rn(fh, gh[k]);
-        const float Fl = __fmaf_rn(fh, gl[k], __fmaf_rn(fl, gh[k], __fmaf_rn(fh, gh[k], -Fh)));
-        const float t = __fadd_rn(ah[k], Fh);
-        const float err = two_sum_err(ah[k], Fh, t);
-        ah[k] = t;
-        al[k] = __fadd_rn(al[k], __fadd_rn(err, Fl));
-    }
-    return true;
-}
-
-// FP64 pair in physical units, G-less (the Numba loop arithmetic).
-template <int DIM>
-__device__ __forceinline__ void pair_fp64(double x, double y, double z, double px, double py,
-                                          double pz, double pm, double eps2, double* a64)
-{
-    const double dx = __dsub_rn(px, x), dy = __dsub_rn(py, y);
-    const double dz = DIM == 3 ? __dsub_rn(pz, z) : 0.0;
-    double r2 = __dmul_rn(dx, dx);
-    r2 = __dadd_rn(r2, __dmul_rn(dy, dy));
-    if (DIM == 3) r2 = __dadd_rn(r2, __dmul_rn(dz, dz));
-    r2 = __dadd_rn(r2, eps2);
-    if (r2 == 0.0) return;
-    const double ri = __ddiv_rn(1.0, __dsqrt_rn(r2));
-    const double f = __dmul_rn(pm, __dmul_rn(__dmul_rn(ri, ri), ri));
-    a64[0] = __dadd_rn(a64[0], __dmul_rn(f, dx));
-    a64[1] = __dadd_rn(a64[1], __dmul_rn(f, dy));
-    if (DIM == 3) a64[2] = __dadd_rn(a64[2], __dmul_rn(f, dz));
-}
-
-// Exact opening test (bh.py:576-601), same arithmetic as k_traverse_exact.
-template <int DIM>
-__device__ __forceinline__ bool open_exact64(double x, double y, double z, const NodeCM& cm,
-                                             double size, double theta)
-{
-    double dx = __dsub_rn(x, cm.x), dy = __dsub_rn(y, cm.y);
-    double s;
-    if (DIM == 3) {
-        double dz = __dsub_rn(z, cm.z);
-        s = __fma_rn(dz, dz, __fma_rn(dy, dy, __dmul_rn(dx, dx)));
-    } else {
-        s = __fma_rn(dy, dy, __dmul_rn(dx, dx));
-    }
-    double d = __dsqrt_rn(s);
-    if (d == 0.0) return true;
-    return __ddiv_rn(size, d) >= theta;
 }
 
 // ---------------------------------------------------------------------------
@@ -494,31 +320,6 @@ k_traverse_fast(TreeDev t, FastTree ft, FastArgs a)
 // Kahan compensation.  FP64 stays in the tree build (bounding box, Morton
 // keys, masses and centres of mass) and in the final scaling.
 // ---------------------------------------------------------------------------
-// Displacement from the hi parts (exact on the grid) plus the lo parts
-// (exact on their grid), rounded once: FP32-relative accuracy everywhere in
-// the box, also in dense regions far from the box centre.
-template <int DIM>
-__device__ __forceinline__ void pair_f32(const float* Th, const float* Tl, float4 sh, float4 sl,
-                                         float e2, float* acc, float* cmp)
-{
-    const float d0 = __fadd_rn(__fsub_rn(sh.x, Th[0]), __fsub_rn(sl.x, Tl[0]));
-    const float d1 = __fadd_rn(__fsub_rn(sh.y, Th[1]), __fsub_rn(sl.y, Tl[1]));
-    const float d2 = DIM == 3 ? __fadd_rn(__fsub_rn(sh.z, Th[2]), __fsub_rn(sl.z, Tl[2])) : 0.0f;
-    float r2 = fmaf(d1, d1, fmaf(d0, d0, e2));
-    if (DIM == 3) r2 = fmaf(d2, d2, r2);
-    if (!(r2 > 0.0f)) return;                  // r^2 + eps^2 == 0: no term (kernels.py:62-63)
-    const float ri = rsqrtf(r2);
-    const float f = sh.w * (ri * ri * ri);
-    const float d[3] = {d0, d1, d2};
-#pragma unroll
-    for (int k = 0; k < DIM; k++) {            // Kahan compensated sum
-        const float y = __fsub_rn(__fmul_rn(f, d[k]), cmp[k]);
-        const float t = __fadd_rn(acc[k], y);
-        cmp[k] = __fsub_rn(__fsub_rn(t, acc[k]), y);
-        acc[k] = t;
-    }
-}
-
 template <int DIM>
 __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, const FastArgs& a,
                                          int w, int lane, bool valid, int64_t me_sorted,

@@ -14,7 +14,10 @@ a seed with numpy's PCG64 ``default_rng``:
 * ``uniform_cube``: uniform in a centred cube of the given side.
 * ``galaxy``: 70 % exponential disc (radial scale ``rd`` drawn from
   Gamma(2, rd), sech^2 vertical profile z = z0 * atanh(2u - 1)) and 30 %
-  Hernquist bulge (r = a sqrt(u) / (1 - sqrt(u))), equal masses 1/N.
+  Hernquist bulge (r = a sqrt(u) / (1 - sqrt(u)), radii beyond ``rmax * a``
+  redrawn as for the Plummer sphere: untruncated, the sampler's tail puts a
+  few particles at 1e6 a and inflates the box by orders of magnitude), equal
+  masses 1/N.
 """
 from __future__ import annotations
 
@@ -75,7 +78,7 @@ def uniform_cube(n: int, seed: int = 0, side: float = 10.0, dim: int = 3):
 
 
 def galaxy(n: int, seed: int = 0, rd: float = 3.0, z0: float = 0.3, a_bulge: float = 0.5,
-           disc_fraction: float = 0.7):
+           disc_fraction: float = 0.7, rmax: float = 20.0):
     rng = np.random.default_rng(seed)
     nd = int(round(disc_fraction * n))
     nb = n - nd
@@ -85,10 +88,14 @@ def galaxy(n: int, seed: int = 0, rd: float = 3.0, z0: float = 0.3, a_bulge: flo
     u = np.clip(u, 1e-15, 1.0 - 1e-15)
     z = z0 * np.arctanh(2.0 * u - 1.0)
     disc = np.stack([R * np.cos(phi), R * np.sin(phi), z], axis=1)
-    ub = rng.uniform(0.0, 1.0, nb)
-    ub = np.clip(ub, 0.0, 1.0 - 1e-12)
-    s = np.sqrt(ub)
-    rb = a_bulge * s / (1.0 - s)
+    rb = np.empty(nb)
+    todo = np.arange(nb)
+    while len(todo):
+        s = np.sqrt(rng.uniform(0.0, 1.0, len(todo)))
+        rr = a_bulge * s / np.maximum(1.0 - s, 1e-300)
+        ok = rr <= rmax * a_bulge
+        rb[todo[ok]] = rr[ok]
+        todo = todo[~ok]
     bulge = _isotropic(rng, nb) * rb[:, None]
     pos = np.concatenate([disc, bulge], axis=0)
     return pos, np.full(n, 1.0 / n)
