@@ -58,6 +58,13 @@ SIGNATURES = {
     "bhut_morton_argsort": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),
     "bhut_direct_accelerations": (_INT, [_VP, _VP, _I64, _INT, _VP, _I64, _D, _D, _VP, _VP]),
     "bhut_morton_argsort_noalloc": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),
+    "bhut_batch_create": (_INT, [_INT, _INT, _VP, ctypes.POINTER(_VP)]),
+    "bhut_batch_configure": (_INT, [_VP, _INT, _INT, _INT, _INT]),
+    "bhut_batch_load": (_INT, [_VP, _VP, _VP, _VP, _I64]),
+    "bhut_batch_solve": (_INT, [_VP, _D, _D, _D, _VP]),
+    "bhut_batch_info": (_INT, [_VP] + [ctypes.POINTER(_I64)] * 4),
+    "bhut_batch_stats": (_INT, [_VP] + [ctypes.POINTER(_I64)] * 3),
+    "bhut_batch_destroy": (None, [_VP]),
 }
 
 _lock = threading.Lock()

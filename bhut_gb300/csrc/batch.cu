@@ -1,0 +1,875 @@
+// Batched form: many independent N-body systems solved in one pass.
+//
+// The systems are concatenated (CSR offsets).  The build is segmented:
+//   k_seg_bbox        one block per system: box + max |m|
+//   k_seg_morton      one block per system: Morton keys in that system's box
+//   radix_sort_pairs  by Morton key, then (stable) by system id
+//   k_gather_sorted   sorted SoA (global)
+//   k_seg_topology    one block per system: the count-split topology of
+//                     bhut/tree/build.py:110-212 for that system's N, ids
+//                     offset into one forest (cached while the layout holds)
+//   k_bottom_up       shared with the single-tree engine (leaves of all
+//                     systems climb their own tree)
+//   k_seg_frames      one block per system: normalisation frame, float-float
+//                     particles and nodes
+// and the traversal is one persistent kernel: every warp pulls
+// (system, target chunk) tasks from a global atomic counter (heaviest systems
+// first) until the queue is empty -- no warp waits on another.  Each task is
+// the warp-cooperative walk of the single-tree kernels, rooted at the
+// system's root; with TPW = 16 two lanes share a target and split its pair
+// loop.  All launches of a solve can be captured in one CUDA graph.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "../../include/bhut_gb300.h"
+#include "fast.cuh"
+
+namespace bhut {
+bool is_device_pointer(const void* p);
+}
+
+using namespace bhut;
+
+namespace {
+
+constexpr int kSegThreads = 256;
+constexpr int kBatchWarps = 4;
+constexpr int kBatchThreads = kBatchWarps * kWarp;
+
+// ---------------------------------------------------------------------------
+// segmented build kernels
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kSegThreads)
+k_seg_bbox(const double* __restrict__ pos, const double* __restrict__ mass,
+           const int64_t* __restrict__ off, int dim, double* __restrict__ box,
+           unsigned* __restrict__ err)
+{
+    const int s = blockIdx.x;
+    const int64_t p0 = off[s], p1 = off[s + 1];
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    double mm = 0.0;
+    bool bad = false;
+    for (int64_t i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
+        for (int d = 0; d < dim; d++) {
+            const double v = pos[i * dim + d];
+            bad |= !isfinite(v);
+            lo[d] = v < lo[d] ? v : lo[d];
+            hi[d] = v > hi[d] ? v : hi[d];
+        }
+        const double am = fabs(mass[i]);
+        bad |= !isfinite(am);
+        mm = am > mm ? am : mm;
+    }
+    __shared__ double red[kSegThreads / 32][7];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int d = 0; d < 3; d++) {
+            const double a = __shfl_down_sync(0xffffffffu, lo[d], o);
+            const double b = __shfl_down_sync(0xffffffffu, hi[d], o);
+            lo[d] = a < lo[d] ? a : lo[d];
+            hi[d] = b > hi[d] ? b : hi[d];
+        }
+        const double c = __shfl_down_sync(0xffffffffu, mm, o);
+        mm = c > mm ? c : mm;
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(err, kErrNonFinite);
+    if (lane == 0) {
+        for (int d = 0; d < 3; d++) { red[warp][d] = lo[d]; red[warp][3 + d] = hi[d]; }
+        red[warp][6] = mm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kSegThreads / 32; w++) {
+            for (int d = 0; d < 3; d++) {
+                lo[d] = red[w][d] < lo[d] ? red[w][d] : lo[d];
+                hi[d] = red[w][3 + d] > hi[d] ? red[w][3 + d] : hi[d];
+            }
+            mm = red[w][6] > mm ? red[w][6] : mm;
+        }
+        for (int d = 0; d < 3; d++) { box[s * 8 + d] = lo[d]; box[s * 8 + 3 + d] = hi[d]; }
+        box[s * 8 + 6] = mm;
+    }
+}
+
+__global__ void __launch_bounds__(kSegThreads)
+k_seg_morton(const double* __restrict__ pos, const int64_t* __restrict__ off, int dim,
+             const double* __restrict__ box, uint64_t* __restrict__ keys,
+             int32_t* __restrict__ idx, int32_t* __restrict__ sys_of)
+{
+    const int s = blockIdx.x;
+    const int64_t p0 = off[s], p1 = off[s + 1];
+    const double* bx = box + s * 8;
+    double pmin[3], ext[3], offs[3];
+    for (int d = 0; d < 3; d++) { pmin[d] = 0.0; ext[d] = 1.0; offs[d] = 0.0; }
+    for (int d = 0; d < dim; d++) {
+        pmin[d] = bx[d];
+        const double e = __dsub_rn(bx[3 + d], bx[d]);
+        ext[d] = e <= 0 ? 1.0 : e;
+        offs[d] = e <= 0 ? 0.5 : 0.0;
+    }
+    for (int64_t i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
+        uint64_t key;
+        if (dim == 3) {
+            key = morton3(quantise(pos[3 * i], pmin[0], ext[0], offs[0]),
+                          quantise(pos[3 * i + 1], pmin[1], ext[1], offs[1]),
+                          quantise(pos[3 * i + 2], pmin[2], ext[2], offs[2]));
+        } else {
+            key = morton2(quantise(pos[2 * i], pmin[0], ext[0], offs[0]),
+                          quantise(pos[2 * i + 1], pmin[1], ext[1], offs[1]));
+        }
+        keys[i] = key;
+        idx[i] = (int32_t)i;
+        sys_of[i] = s;
+    }
+}
+
+__global__ void k_seg_key2(const int32_t* __restrict__ perm, const int32_t* __restrict__ sys_of,
+                           int64_t n, uint64_t* __restrict__ key2)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        key2[i] = (uint64_t)sys_of[perm[i]];
+}
+
+// One block per system.  Thread 0 builds the per-depth tables of the
+// closed form (see k_topology in build.cu) in shared memory; the block then
+// walks that system's BFS slots.
+__global__ void __launch_bounds__(kSegThreads)
+k_seg_topology(const int64_t* __restrict__ part_off, const int64_t* __restrict__ node_off,
+               const int64_t* __restrict__ leaf_off, int leaf_size,
+               int32_t* __restrict__ first_child, int32_t* __restrict__ start,
+               int32_t* __restrict__ count, int32_t* __restrict__ parent,
+               int32_t* __restrict__ leaf_list, unsigned* __restrict__ err)
+{
+    const int s = blockIdx.x;
+    const int64_t n = part_off[s + 1] - part_off[s];
+    const int64_t L = leaf_size;
+    __shared__ int64_t cnt_lo[kMaxDepth];
+    __shared__ int64_t internal[kMaxDepth][2];
+    __shared__ int depth_s;
+    __shared__ unsigned leaf_ctr;
+    if (threadIdx.x == 0) {
+        int depth = 0;
+        while (((n + (1ll << depth) - 1) >> depth) > L && depth < kMaxDepth - 2) depth++;
+        depth_s = depth;
+        for (int d = 0; d <= depth + 1; d++) cnt_lo[d] = n >> d;
+        for (int d = depth + 1; d >= 0; d--) {
+            for (int v = 0; v < 2; v++) {
+                const int64_t c = cnt_lo[d] + v;
+                if (c <= L) { internal[d][v] = 0; continue; }
+                const int64_t h = c / 2, r = c - h, lo = cnt_lo[d + 1];
+                internal[d][v] = 1 + internal[d + 1][h - lo] + internal[d + 1][r - lo];
+            }
+        }
+        leaf_ctr = 0;
+    }
+    __syncthreads();
+    const int depth = depth_s;
+    const int64_t nodes = node_off[s + 1] - node_off[s];
+    const int64_t leaves = leaf_off[s + 1] - leaf_off[s];
+    const int64_t slots = (2ll << depth) - 1;
+    const int64_t nb = node_off[s], pb = part_off[s];
+    for (int64_t slot = threadIdx.x; slot < slots; slot += blockDim.x) {
+        const int d = 63 - __clzll((unsigned long long)(slot + 1));
+        const int64_t j = slot + 1 - (1ll << d);
+        int64_t c = n, st = 0, k = 0, id = 0, par = -1;
+        bool exists = true;
+        for (int t = 0; t < d; t++) {
+            if (c <= L) { exists = false; break; }
+            const int bit = (int)((j >> (d - 1 - t)) & 1);
+            const int64_t half = c / 2, rc = c - half;
+            par = id;
+            if (bit == 0) {
+                id = 2 * k + 1;
+                k = k + 1 + internal[t + 1][rc - cnt_lo[t + 1]];
+                c = half;
+            } else {
+                id = 2 * k + 2;
+                k = k + 1;
+                st += half;
+                c = rc;
+            }
+        }
+        if (!exists) continue;
+        if (id >= nodes || st + c > n) { atomicOr(err, kErrBadNode); continue; }
+        start[nb + id] = (int32_t)(pb + st);
+        count[nb + id] = (int32_t)c;
+        parent[nb + id] = par < 0 ? -1 : (int32_t)(nb + par);
+        if (c <= L) {
+            first_child[nb + id] = -1;
+            const unsigned li = atomicAdd(&leaf_ctr, 1u);
+            if (li < leaves) leaf_list[leaf_off[s] + li] = (int32_t)(nb + id);
+            else atomicOr(err, kErrBadNode);
+        } else {
+            first_child[nb + id] = (int32_t)(nb + 2 * k + 1);
+        }
+    }
+}
+
+// One block per system: frame, float-float particles and nodes.
+__global__ void __launch_bounds__(kSegThreads)
+k_seg_frames(TreeDev t, const int64_t* __restrict__ part_off, const int64_t* __restrict__ node_off,
+             const double* __restrict__ box, const double* __restrict__ center,
+             FastFrame* __restrict__ frames, float4* __restrict__ ph, float4* __restrict__ pl,
+             float4* __restrict__ nh, float4* __restrict__ nl, float* __restrict__ nsize,
+             float* __restrict__ ndelta)
+{
+    const int s = blockIdx.x;
+    const int dim = t.dim;
+    __shared__ FastFrame f;
+    if (threadIdx.x == 0) {
+        frame_from_box(box + s * 8, dim, &f);
+        frames[s] = f;
+    }
+    __syncthreads();
+    for (int64_t i = part_off[s] + threadIdx.x; i < part_off[s + 1]; i += blockDim.x) {
+        float4 h, l;
+        split_grid(__dmul_rn(__dsub_rn(t.sx[i], f.c[0]), f.s), h.x, l.x);
+        split_grid(__dmul_rn(__dsub_rn(t.sy[i], f.c[1]), f.s), h.y, l.y);
+        if (dim == 3) split_grid(__dmul_rn(__dsub_rn(t.sz[i], f.c[2]), f.s), h.z, l.z);
+        else h.z = l.z = 0.0f;
+        split_plain(__dmul_rn(t.sm[i], f.ms), h.w, l.w);
+        ph[i] = h;
+        pl[i] = l;
+    }
+    for (int64_t k = node_off[s] + threadIdx.x; k < node_off[s + 1]; k += blockDim.x) {
+        const NodeCM c = t.cm[k];
+        float4 h, l;
+        split_grid(__dmul_rn(__dsub_rn(c.x, f.c[0]), f.s), h.x, l.x);
+        split_grid(__dmul_rn(__dsub_rn(c.y, f.c[1]), f.s), h.y, l.y);
+        if (dim == 3) split_grid(__dmul_rn(__dsub_rn(c.z, f.c[2]), f.s), h.z, l.z);
+        else h.z = l.z = 0.0f;
+        split_plain(__dmul_rn(c.w, f.ms), h.w, l.w);
+        nh[k] = h;
+        nl[k] = l;
+        nsize[k] = __double2float_rn(__dmul_rn(t.size[k], f.s));
+        double dd = 0.0;
+        for (int d = 0; d < dim; d++) {
+            const double cc = d == 0 ? c.x : (d == 1 ? c.y : c.z);
+            const double v = cc - center[k * dim + d];
+            dd += v * v;
+        }
+        ndelta[k] = __double2float_ru(sqrt(dd) * f.s);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// persistent traversal
+// ---------------------------------------------------------------------------
+struct BatchDev {
+    TreeDev t;                    // global forest (node ids, particles)
+    const int64_t* part_off;
+    const int64_t* node_off;
+    const FastFrame* frames;
+    const float4* ph;
+    const float4* pl;
+    const float4* nh;
+    const float4* nl;
+    const float* nsize;
+    const float* ndelta;
+};
+
+struct BatchArgs {
+    const int2* tasks;            // (system, chunk), heaviest systems first
+    int ntasks;
+    unsigned* counter;            // task ticket counter (zeroed before launch)
+    double theta, eps, G;
+    int mac;
+    double* out;                  // (N_total, dim), input order
+    unsigned* err;
+    unsigned long long* stats;
+};
+
+template <int DIM, bool FP32, int TPW>
+__global__ void __launch_bounds__(kBatchThreads)
+k_batch_traverse(BatchDev b, BatchArgs a)
+{
+    constexpr int LPT = kWarp / TPW;            // lanes per target
+    __shared__ int2 stack[kBatchWarps][kStackDepth];
+    __shared__ float4 sh[kBatchWarps][kWarp], sl[kBatchWarps][kWarp];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int sub = lane % LPT;
+    const unsigned FULL = 0xffffffffu;
+    const TreeDev& t = b.t;
+    const float theta_f = (float)a.theta;
+    const double eps2 = __dmul_rn(a.eps, a.eps);
+    unsigned long long tot[5] = {0, 0, 0, 0, 0};
+
+    while (true) {
+        int task = 0;
+        if (lane == 0) task = (int)atomicAdd(a.counter, 1u);
+        task = __shfl_sync(FULL, task, 0);
+        if (task >= a.ntasks) break;
+        const int2 tk = a.tasks[task];
+        const int sys = tk.x;
+        const int64_t p1 = b.part_off[sys + 1];
+        const int64_t i = b.part_off[sys] + (int64_t)tk.y * TPW + lane / LPT;
+        const bool valid = i < p1;
+        const FastFrame fr = b.frames[sys];
+        const int root = (int)b.node_off[sys];
+        const double es = __dmul_rn(a.eps, fr.s);
+        const double e2 = __dmul_rn(es, es);
+        const float e2h = __double2float_rn(e2);
+        const float e2l = __double2float_rn(__dsub_rn(e2, (double)e2h));
+
+        float Th[3] = {0.f, 0.f, 0.f}, Tl[3] = {0.f, 0.f, 0.f};
+        double x = 0.0, y = 0.0, z = 0.0;
+        if (valid) {
+            const float4 h = b.ph[i], l = b.pl[i];
+            Th[0] = h.x; Th[1] = h.y; Th[2] = h.z;
+            Tl[0] = l.x; Tl[1] = l.y; Tl[2] = l.z;
+            if (!FP32) {
+                x = t.sx[i];
+                y = t.sy[i];
+                z = DIM == 3 ? t.sz[i] : 0.0;
+            }
+        }
+        float ah[3] = {0.f, 0.f, 0.f}, al[3] = {0.f, 0.f, 0.f};   // ff sum, or (sum, Kahan comp)
+        double a64[3] = {0.0, 0.0, 0.0};
+        unsigned cnt[5] = {0, 0, 0, 0, 0};
+        bool overflow = false;
+
+        const unsigned live = __ballot_sync(FULL, valid);
+        if (lane == 0) stack[w][0] = make_int2(root, (int)live);
+        int sp = 1;
+        __syncwarp();
+        while (sp > 0) {
+            const int2 e = stack[w][--sp];
+            __syncwarp();
+            const int node = e.x;
+            const bool act = ((unsigned)e.y >> lane) & 1u;
+            cnt[2] += act && sub == 0;
+            if ((__double_as_longlong(__ldg(&t.cm[node].w)) << 1) == 0) continue;
+            const int fc = t.first_child[node];
+            if (fc < 0) {
+                const int s0 = t.start[node], c = t.count[node];
+                for (int bb = 0; bb < c; bb += kWarp) {
+                    const int jj = bb + lane;
+                    if (jj < c) {
+                        sh[w][lane] = b.ph[s0 + jj];
+                        sl[w][lane] = b.pl[s0 + jj];
+                    }
+                    __syncwarp();
+                    const int cn = min(kWarp, c - bb);
+                    if (act) {
+                        if (sub == 0) cnt[0] += cn - (i >= s0 + bb && i < s0 + bb + cn);
+                        for (int q = sub; q < cn; q += LPT) {
+                            if (FP32) {
+                                pair_f32<DIM>(Th, Tl, sh[w][q], sl[w][q], e2h, ah, al);
+                            } else if (!pair_ff<DIM, false>(Th, Tl, sh[w][q], sl[w][q], e2h, e2l,
+                                                            ah, al)) {
+                                const int gi = s0 + bb + q;
+                                pair_fp64<DIM>(x, y, z, t.sx[gi], t.sy[gi],
+                                               DIM == 3 ? t.sz[gi] : 0.0, t.sm[gi], eps2, a64);
+                                cnt[4]++;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+                if (!FP32 && act) {
+#pragma unroll
+                    for (int k = 0; k < DIM; k++) {
+                        const float hs = __fadd_rn(ah[k], al[k]);
+                        al[k] = __fsub_rn(al[k], __fsub_rn(hs, ah[k]));
+                        ah[k] = hs;
+                    }
+                }
+            } else {
+                bool open = false;
+                float4 nhv = make_float4(0.f, 0.f, 0.f, 0.f), nlv = nhv;
+                if (act) {
+                    nhv = b.nh[node];
+                    nlv = b.nl[node];
+                    float d2 = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < DIM; k++) {
+                        const float d = __fadd_rn(__fsub_rn(comp(nhv, k), Th[k]),
+                                                  __fsub_rn(comp(nlv, k), Tl[k]));
+                        d2 = fmaf(d, d, d2);
+                    }
+                    const float dist = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+                    const float size_f = b.nsize[node];
+                    if (FP32) {
+                        open = a.mac == 1 ? size_f >= theta_f * (dist - b.ndelta[node])
+                                          : (dist == 0.0f || size_f >= theta_f * dist);
+                    } else {
+                        const float td = theta_f * dist;
+                        const float band = theta_f * fmaf(kBandRel, dist, 2.0f * kBandAbs);
+                        if (size_f >= td + band) open = true;
+                        else if (size_f < td - band) open = false;
+                        else {
+                            open = open_exact64<DIM>(x, y, z, t.cm[node], t.size[node], a.theta);
+                            cnt[3]++;
+                        }
+                    }
+                }
+                const unsigned omask = __ballot_sync(FULL, act && open);
+                if (act && !open && sub == 0) {
+                    if (FP32) {
+                        pair_f32<DIM>(Th, Tl, nhv, nlv, e2h, ah, al);
+                    } else if (!pair_ff<DIM, false>(Th, Tl, nhv, nlv, e2h, e2l, ah, al)) {
+                        const NodeCM cm = t.cm[node];
+                        pair_fp64<DIM>(x, y, z, cm.x, cm.y, cm.z, cm.w, eps2, a64);
+                        cnt[4]++;
+                    }
+                    cnt[1]++;
+                }
+                if (omask) {
+                    if (sp + 2 > kStackDepth) { overflow = true; break; }
+                    if (lane == 0) {
+                        stack[w][sp] = make_int2(fc, (int)omask);
+                        stack[w][sp + 1] = make_int2(fc + 1, (int)omask);
+                    }
+                    sp += 2;
+                    __syncwarp();
+                }
+            }
+        }
+        if (overflow && lane == 0) atomicOr(a.err, kErrStackOverflow);
+        // fold the lanes that share a target
+        if (LPT == 2) {
+#pragma unroll
+            for (int k = 0; k < DIM; k++) {
+                const float oh = __shfl_down_sync(FULL, ah[k], 1);
+                const float ol = __shfl_down_sync(FULL, al[k], 1);
+                const double o64 = __shfl_down_sync(FULL, a64[k], 1);
+                if (FP32) {
+                    ah[k] = __fadd_rn(ah[k], oh);
+                    al[k] = __fadd_rn(al[k], ol);
+                } else {
+                    const float s2 = __fadd_rn(ah[k], oh);
+                    al[k] = __fadd_rn(__fadd_rn(al[k], ol), two_sum_err(ah[k], oh, s2));
+                    ah[k] = s2;
+                }
+                a64[k] = a64[k] + o64;
+            }
+        }
+        for (int k = 0; k < 5; k++) tot[k] += cnt[k];
+        if (valid && sub == 0) {
+            const double conv = __dmul_rn(fr.conv, a.G);
+            const int64_t o = t.perm[i];
+#pragma unroll
+            for (int k = 0; k < DIM; k++) {
+                const double v = FP32 ? __dsub_rn((double)ah[k], (double)al[k])
+                                      : __dadd_rn((double)ah[k], (double)al[k]);
+                a.out[o * DIM + k] = __dadd_rn(__dmul_rn(v, conv), __dmul_rn(a64[k], a.G));
+            }
+        }
+    }
+    if (a.stats) {
+        for (int k = 0; k < 5; k++) {
+            unsigned long long v = tot[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+            if (lane == 0 && v) atomicAdd(&a.stats[k], v);
+        }
+    }
+}
+
+inline size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// handle
+// ---------------------------------------------------------------------------
+struct BufB {
+    void* p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t need, cudaStream_t s)
+    {
+        if (need <= bytes && p) return kOk;
+        if (p) { cudaFreeAsync(p, s); p = nullptr; bytes = 0; }
+        cudaError_t e = cudaMallocAsync(&p, need < 256 ? 256 : need, s);
+        if (e != cudaSuccess) { p = nullptr; return cuda_status(e, "cudaMallocAsync"); }
+        bytes = need < 256 ? 256 : need;
+        return kOk;
+    }
+    void release(cudaStream_t s) { if (p) cudaFreeAsync(p, s); p = nullptr; bytes = 0; }
+    template <class T> T* as() const { return (T*)p; }
+};
+
+struct bhut_batch {
+    int dim = 3, leaf = 32, form = BHUT_FORM_FP32, mac = 0, tpw = 32;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int64_t nsys = 0, ntot = 0, mtot = 0, ltot = 0;
+    std::vector<int64_t> part_off, node_off, leaf_off;
+    std::vector<int2> tasks;
+    bool layout_valid = false, built = false, topo_valid = false;
+    BufB pos, mass, d_part_off, d_node_off, d_leaf_off, d_tasks, keys, perm, sys_of, key2,
+        sx, sy, sz, sm, cm, size, center, half, lo, hi, first_child, start, count, parent,
+        leaf_list, arrive, sort_scratch, box, frames, ph, pl, nh, nl, nsize, ndelta, counter,
+        err, stats, out;
+    unsigned long long last_stats[5] = {0, 0, 0, 0, 0};
+    cudaGraphExec_t graph = nullptr;
+    bool use_graph = false;
+    double g_theta = -1, g_eps = -1, g_G = 0;
+    double* g_out = nullptr;
+
+    BufB* all[46] = {&pos, &mass, &d_part_off, &d_node_off, &d_leaf_off, &d_tasks, &keys, &perm,
+                     &sys_of, &key2, &sx, &sy, &sz, &sm, &cm, &size, &center, &half, &lo, &hi,
+                     &first_child, &start, &count, &parent, &leaf_list, &arrive, &sort_scratch,
+                     &box, &frames, &ph, &pl, &nh, &nl, &nsize, &ndelta, &counter, &err, &stats,
+                     &out, nullptr};
+
+    TreeDev dev() const
+    {
+        TreeDev t;
+        t.dim = dim; t.leaf_size = leaf; t.n = ntot; t.m = mtot;
+        t.sx = sx.as<double>(); t.sy = sy.as<double>(); t.sz = sz.as<double>();
+        t.sm = sm.as<double>(); t.perm = perm.as<int32_t>(); t.cm = cm.as<NodeCM>();
+        t.size = size.as<double>(); t.first_child = first_child.as<int32_t>();
+        t.start = start.as<int32_t>(); t.count = count.as<int32_t>();
+        return t;
+    }
+};
+
+namespace {
+
+void drop_graph(bhut_batch* b)
+{
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+}
+
+// Task list: (system, chunk of tpw targets), heaviest systems first so that
+// the queue drains evenly.
+int plan_tasks(bhut_batch* b)
+{
+    std::vector<std::pair<int64_t, int>> order;
+    for (int64_t s = 0; s < b->nsys; s++)
+        order.push_back({b->part_off[s + 1] - b->part_off[s], (int)s});
+    std::stable_sort(order.begin(), order.end(),
+                     [](const std::pair<int64_t, int>& x, const std::pair<int64_t, int>& y) {
+                         return x.first > y.first;
+                     });
+    b->tasks.clear();
+    for (auto& o : order) {
+        const int64_t chunks = (o.first + b->tpw - 1) / b->tpw;
+        for (int64_t c = 0; c < chunks; c++) b->tasks.push_back(make_int2(o.second, (int)c));
+    }
+    BHUT_TRY(b->d_tasks.ensure(sizeof(int2) * b->tasks.size(), b->stream));
+    BHUT_CUDA(cudaMemcpyAsync(b->d_tasks.p, b->tasks.data(), sizeof(int2) * b->tasks.size(),
+                              cudaMemcpyHostToDevice, b->stream));
+    BHUT_CUDA(cudaStreamSynchronize(b->stream));   // the host vector is reused
+    return kOk;
+}
+
+// Host plan: node and leaf counts of every system, buffers, task list.
+int plan_layout(bhut_batch* b, const int64_t* offsets, int64_t nsys)
+{
+    b->part_off.assign(offsets, offsets + nsys + 1);
+    b->node_off.assign(nsys + 1, 0);
+    b->leaf_off.assign(nsys + 1, 0);
+    for (int64_t s = 0; s < nsys; s++) {
+        const int64_t n = offsets[s + 1] - offsets[s];
+        if (n <= 0) { set_error("system %lld has no particles", (long long)s); return kInvalid; }
+        TopoTables tt;
+        BHUT_TRY(make_topo_tables(n, b->leaf, &tt));
+        b->node_off[s + 1] = b->node_off[s] + tt.num_nodes;
+        b->leaf_off[s + 1] = b->leaf_off[s] + tt.num_leaves;
+    }
+    b->nsys = nsys;
+    b->ntot = offsets[nsys];
+    b->mtot = b->node_off[nsys];
+    b->ltot = b->leaf_off[nsys];
+    if (b->ntot > 0x7fffffffLL || b->mtot > 0x7fffffffLL) {
+        set_error("batch too large: at most 2^31-1 particles and nodes");
+        return kInvalid;
+    }
+    cudaStream_t s = b->stream;
+    const size_t ntot = (size_t)b->ntot, mtot = (size_t)b->mtot;
+    BHUT_TRY(b->d_part_off.ensure(sizeof(int64_t) * (nsys + 1), s));
+    BHUT_TRY(b->d_node_off.ensure(sizeof(int64_t) * (nsys + 1), s));
+    BHUT_TRY(b->d_leaf_off.ensure(sizeof(int64_t) * (nsys + 1), s));
+    BHUT_CUDA(cudaMemcpyAsync(b->d_part_off.p, b->part_off.data(), sizeof(int64_t) * (nsys + 1),
+                              cudaMemcpyHostToDevice, s));
+    BHUT_CUDA(cudaMemcpyAsync(b->d_node_off.p, b->node_off.data(), sizeof(int64_t) * (nsys + 1),
+                              cudaMemcpyHostToDevice, s));
+    BHUT_CUDA(cudaMemcpyAsync(b->d_leaf_off.p, b->leaf_off.data(), sizeof(int64_t) * (nsys + 1),
+                              cudaMemcpyHostToDevice, s));
+    BHUT_TRY(plan_tasks(b));
+    const int dim = b->dim;
+    BHUT_TRY(b->pos.ensure(sizeof(double) * ntot * dim, s));
+    BHUT_TRY(b->mass.ensure(sizeof(double) * ntot, s));
+    BHUT_TRY(b->keys.ensure(sizeof(uint64_t) * ntot, s));
+    BHUT_TRY(b->key2.ensure(sizeof(uint64_t) * ntot, s));
+    BHUT_TRY(b->perm.ensure(sizeof(int32_t) * ntot, s));
+    BHUT_TRY(b->sys_of.ensure(sizeof(int32_t) * ntot, s));
+    for (BufB* x : {&b->sx, &b->sy, &b->sz, &b->sm}) BHUT_TRY(x->ensure(sizeof(double) * ntot, s));
+    BHUT_TRY(b->ph.ensure(sizeof(float4) * ntot, s));
+    BHUT_TRY(b->pl.ensure(sizeof(float4) * ntot, s));
+    BHUT_TRY(b->out.ensure(sizeof(double) * ntot * dim, s));
+    BHUT_TRY(b->cm.ensure(sizeof(NodeCM) * mtot, s));
+    for (BufB* x : {&b->size, &b->half}) BHUT_TRY(x->ensure(sizeof(double) * mtot, s));
+    BHUT_TRY(b->center.ensure(sizeof(double) * mtot * dim, s));
+    BHUT_TRY(b->lo.ensure(sizeof(double) * mtot * 3, s));
+    BHUT_TRY(b->hi.ensure(sizeof(double) * mtot * 3, s));
+    for (BufB* x : {&b->first_child, &b->start, &b->count, &b->parent})
+        BHUT_TRY(x->ensure(sizeof(int32_t) * mtot, s));
+    BHUT_TRY(b->arrive.ensure(sizeof(unsigned) * mtot, s));
+    BHUT_TRY(b->leaf_list.ensure(sizeof(int32_t) * b->ltot, s));
+    BHUT_TRY(b->nh.ensure(sizeof(float4) * mtot, s));
+    BHUT_TRY(b->nl.ensure(sizeof(float4) * mtot, s));
+    BHUT_TRY(b->nsize.ensure(sizeof(float) * mtot, s));
+    BHUT_TRY(b->ndelta.ensure(sizeof(float) * mtot, s));
+    BHUT_TRY(b->box.ensure(sizeof(double) * 8 * nsys, s));
+    BHUT_TRY(b->frames.ensure(sizeof(FastFrame) * nsys, s));
+    BHUT_TRY(b->sort_scratch.ensure(sort_scratch_bytes(b->ntot), s));
+    BHUT_TRY(b->counter.ensure(sizeof(unsigned) * 4, s));
+    BHUT_TRY(b->err.ensure(sizeof(unsigned), s));
+    BHUT_TRY(b->stats.ensure(sizeof(unsigned long long) * 8, s));
+    BHUT_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(unsigned), s));
+    b->layout_valid = true;
+    b->topo_valid = false;
+    drop_graph(b);
+    return kOk;
+}
+
+int bits_for(int64_t v)
+{
+    int b = 1;
+    while (b < 62 && (1ll << b) <= v) b++;
+    return b;
+}
+
+// All device work of one solve (build + traversal), stream-ordered, no host
+// synchronisation: this is what a CUDA graph captures.
+int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out)
+{
+    cudaStream_t s = b->stream;
+    const int dim = b->dim;
+    const int64_t ns = b->nsys, n = b->ntot;
+    k_seg_bbox<<<(unsigned)ns, kSegThreads, 0, s>>>(b->pos.as<double>(), b->mass.as<double>(),
+                                                    b->d_part_off.as<int64_t>(), dim,
+                                                    b->box.as<double>(), b->err.as<unsigned>());
+    k_seg_morton<<<(unsigned)ns, kSegThreads, 0, s>>>(b->pos.as<double>(),
+                                                      b->d_part_off.as<int64_t>(), dim,
+                                                      b->box.as<double>(), b->keys.as<uint64_t>(),
+                                                      b->perm.as<int32_t>(),
+                                                      b->sys_of.as<int32_t>());
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(2);
+    BHUT_TRY(radix_sort_pairs(b->keys.as<uint64_t>(), b->perm.as<int32_t>(), n,
+                              dim == 3 ? 63 : 42, b->sort_scratch.p, s));
+    if (ns > 1) {
+        k_seg_key2<<<grid_for(n, 256), 256, 0, s>>>(b->perm.as<int32_t>(), b->sys_of.as<int32_t>(),
+                                                     n, b->key2.as<uint64_t>());
+        BHUT_CUDA(cudaGetLastError());
+        note_launches(1);
+        BHUT_TRY(radix_sort_pairs(b->key2.as<uint64_t>(), b->perm.as<int32_t>(), n,
+                                  bits_for(ns - 1), b->sort_scratch.p, s));
+    }
+    BHUT_TRY(launch_gather(b->pos.as<double>(), b->mass.as<double>(), b->perm.as<int32_t>(), n,
+                           dim, b->sx.as<double>(), b->sy.as<double>(), b->sz.as<double>(),
+                           b->sm.as<double>(), s));
+    NodeOut o{b->cm.as<NodeCM>(), b->size.as<double>(), b->center.as<double>(),
+              b->half.as<double>(), b->lo.as<double>(), b->hi.as<double>()};
+    BHUT_TRY(launch_bottom_up(b->dev(), b->leaf_list.as<int32_t>(), b->ltot,
+                              b->first_child.as<int32_t>(), b->start.as<int32_t>(),
+                              b->count.as<int32_t>(), b->parent.as<int32_t>(),
+                              b->arrive.as<unsigned>(), o, false, nullptr, nullptr,
+                              b->err.as<unsigned>(), s));
+    k_seg_frames<<<(unsigned)ns, kSegThreads, 0, s>>>(
+        b->dev(), b->d_part_off.as<int64_t>(), b->d_node_off.as<int64_t>(), b->box.as<double>(),
+        b->center.as<double>(), b->frames.as<FastFrame>(), b->ph.as<float4>(), b->pl.as<float4>(),
+        b->nh.as<float4>(), b->nl.as<float4>(), b->nsize.as<float>(), b->ndelta.as<float>());
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
+    // traversal
+    BHUT_CUDA(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned), s));
+    BHUT_CUDA(cudaMemsetAsync(b->stats.p, 0, sizeof(unsigned long long) * 8, s));
+    BatchDev bd{b->dev(), b->d_part_off.as<int64_t>(), b->d_node_off.as<int64_t>(),
+                b->frames.as<FastFrame>(), b->ph.as<float4>(), b->pl.as<float4>(),
+                b->nh.as<float4>(), b->nl.as<float4>(), b->nsize.as<float>(),
+                b->ndelta.as<float>()};
+    BatchArgs a{b->d_tasks.as<int2>(), (int)b->tasks.size(), b->counter.as<unsigned>(), theta,
+                eps, G, b->mac, out, b->err.as<unsigned>(), b->stats.as<unsigned long long>()};
+    const unsigned grid = 152u * 6u;   // persistent: about one wave of resident blocks
+    const bool fp32 = b->form == BHUT_FORM_FP32;
+    if (dim == 3) {
+        if (fp32 && b->tpw == 32) k_batch_traverse<3, true, 32><<<grid, kBatchThreads, 0, s>>>(bd, a);
+        else if (fp32) k_batch_traverse<3, true, 16><<<grid, kBatchThreads, 0, s>>>(bd, a);
+        else if (b->tpw == 32) k_batch_traverse<3, false, 32><<<grid, kBatchThreads, 0, s>>>(bd, a);
+        else k_batch_traverse<3, false, 16><<<grid, kBatchThreads, 0, s>>>(bd, a);
+    } else {
+        if (fp32) k_batch_traverse<2, true, 32><<<grid, kBatchThreads, 0, s>>>(bd, a);
+        else k_batch_traverse<2, false, 32><<<grid, kBatchThreads, 0, s>>>(bd, a);
+    }
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
+    return kOk;
+}
+
+int ensure_topology(bhut_batch* b)
+{
+    if (b->topo_valid) return kOk;
+    k_seg_topology<<<(unsigned)b->nsys, kSegThreads, 0, b->stream>>>(
+        b->d_part_off.as<int64_t>(), b->d_node_off.as<int64_t>(), b->d_leaf_off.as<int64_t>(),
+        b->leaf, b->first_child.as<int32_t>(), b->start.as<int32_t>(), b->count.as<int32_t>(),
+        b->parent.as<int32_t>(), b->leaf_list.as<int32_t>(), b->err.as<unsigned>());
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
+    b->topo_valid = true;
+    return kOk;
+}
+
+int check_batch_err(bhut_batch* b)
+{
+    unsigned e = 0;
+    BHUT_CUDA(cudaMemcpyAsync(&e, b->err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
+    BHUT_CUDA(cudaMemcpyAsync(b->last_stats, b->stats.p, sizeof(unsigned long long) * 5,
+                              cudaMemcpyDeviceToHost, b->stream));
+    BHUT_CUDA(cudaStreamSynchronize(b->stream));
+    if (!e) return kOk;
+    BHUT_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(unsigned), b->stream));
+    if (e & kErrNonFinite) { set_error("positions and masses must be finite"); return kInvalid; }
+    set_error("device error word 0x%x in batched solve", e);
+    return kDeviceFlag;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bhut_batch_create(int dim, int leaf_size, void* stream, bhut_batch** out)
+{
+    if (!out) { set_error("out is NULL"); return kInvalid; }
+    *out = nullptr;
+    if (dim != 2 && dim != 3) { set_error("dim must be 2 or 3, got %d", dim); return kInvalid; }
+    if (leaf_size <= 0) { set_error("leaf_size must be positive, got %d", leaf_size); return kInvalid; }
+    bhut_batch* b = new bhut_batch();
+    b->dim = dim;
+    b->leaf = leaf_size;
+    if (stream) {
+        b->stream = (cudaStream_t)stream;
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete b; return cuda_status(e, "cudaStreamCreate"); }
+        b->own_stream = true;
+    }
+    *out = b;
+    return kOk;
+}
+
+int bhut_batch_configure(bhut_batch* b, int form, int criterion, int targets_per_warp,
+                         int use_graph)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (form != BHUT_FORM_FAST && form != BHUT_FORM_FP32) {
+        set_error("the batched solver runs form fast or fp32, got %d", form);
+        return kInvalid;
+    }
+    if (criterion != BHUT_MAC_BH && criterion != BHUT_MAC_OFFSET) {
+        set_error("unknown opening criterion %d", criterion);
+        return kInvalid;
+    }
+    if (criterion == BHUT_MAC_OFFSET && form != BHUT_FORM_FP32) {
+        set_error("the offset criterion is available with the fp32 form only");
+        return kInvalid;
+    }
+    if (targets_per_warp != 32 && targets_per_warp != 16) {
+        set_error("targets_per_warp must be 32 or 16, got %d", targets_per_warp);
+        return kInvalid;
+    }
+    if (targets_per_warp == 16 && b->dim != 3) {
+        set_error("targets_per_warp = 16 is built for dim = 3 only");
+        return kInvalid;
+    }
+    const bool retask = targets_per_warp != b->tpw;
+    b->form = form;
+    b->mac = criterion;
+    b->tpw = targets_per_warp;
+    b->use_graph = use_graph != 0;
+    drop_graph(b);
+    if (retask && b->layout_valid) BHUT_TRY(plan_tasks(b));
+    return kOk;
+}
+
+int bhut_batch_load(bhut_batch* b, const double* positions, const double* masses,
+                    const int64_t* offsets, int64_t nsys)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (nsys <= 0 || !offsets || !positions || !masses) { set_error("empty batch"); return kInvalid; }
+    if (offsets[0] != 0) { set_error("offsets[0] must be 0"); return kInvalid; }
+    bool same = b->layout_valid && b->nsys == nsys &&
+                std::memcmp(b->part_off.data(), offsets, sizeof(int64_t) * (nsys + 1)) == 0;
+    if (!same) BHUT_TRY(plan_layout(b, offsets, nsys));
+    cudaStream_t s = b->stream;
+    BHUT_CUDA(cudaMemcpyAsync(b->pos.p, positions, sizeof(double) * b->ntot * b->dim,
+                              is_device_pointer(positions) ? cudaMemcpyDeviceToDevice
+                                                           : cudaMemcpyHostToDevice, s));
+    BHUT_CUDA(cudaMemcpyAsync(b->mass.p, masses, sizeof(double) * b->ntot,
+                              is_device_pointer(masses) ? cudaMemcpyDeviceToDevice
+                                                        : cudaMemcpyHostToDevice, s));
+    b->built = true;
+    return kOk;
+}
+
+int bhut_batch_solve(bhut_batch* b, double theta, double softening, double G, double* out)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (!b->built) { set_error("load systems before solving"); return kNotBuilt; }
+    if (!(theta >= 0)) { set_error("theta must be non-negative, got %g", theta); return kInvalid; }
+    if (!(softening >= 0)) { set_error("softening must be non-negative, got %g", softening); return kInvalid; }
+    BHUT_TRY(ensure_topology(b));
+    const bool dev_out = is_device_pointer(out);
+    double* dst = dev_out ? out : b->out.as<double>();
+    if (b->use_graph) {
+        if (!b->graph || theta != b->g_theta || softening != b->g_eps || G != b->g_G ||
+            dst != b->g_out) {
+            drop_graph(b);
+            cudaGraph_t g;
+            BHUT_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            int st = enqueue_solve(b, theta, softening, G, dst);
+            cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+            if (st != kOk) { if (e == cudaSuccess) cudaGraphDestroy(g); return st; }
+            BHUT_CUDA(e);
+            e = cudaGraphInstantiate(&b->graph, g, 0);
+            cudaGraphDestroy(g);
+            BHUT_CUDA(e);
+            b->g_theta = theta; b->g_eps = softening; b->g_G = G; b->g_out = dst;
+        }
+        BHUT_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    } else {
+        BHUT_TRY(enqueue_solve(b, theta, softening, G, dst));
+    }
+    if (!dev_out)
+        BHUT_CUDA(cudaMemcpyAsync(out, dst, sizeof(double) * b->ntot * b->dim,
+                                  cudaMemcpyDeviceToHost, b->stream));
+    return check_batch_err(b);
+}
+
+int bhut_batch_info(const bhut_batch* b, int64_t* nsys, int64_t* n_total, int64_t* nodes_total,
+                    int64_t* tasks)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (nsys) *nsys = b->nsys;
+    if (n_total) *n_total = b->ntot;
+    if (nodes_total) *nodes_total = b->mtot;
+    if (tasks) *tasks = (int64_t)b->tasks.size();
+    return kOk;
+}
+
+int bhut_batch_stats(const bhut_batch* b, int64_t* p2p, int64_t* m2p, int64_t* visits)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (p2p) *p2p = (int64_t)b->last_stats[0];
+    if (m2p) *m2p = (int64_t)b->last_stats[1];
+    if (visits) *visits = (int64_t)b->last_stats[2];
+    return kOk;
+}
+
+void bhut_batch_destroy(bhut_batch* b)
+{
+    if (!b) return;
+    drop_graph(b);
+    for (BufB* x : b->all) if (x) x->release(b->stream);
+    cudaStreamSynchronize(b->stream);
+    if (b->own_stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+}  // extern "C"

@@ -132,37 +132,6 @@ k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t 
 // ---------------------------------------------------------------------------
 // K2: Morton keys (input order) and the identity payload for the sort.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint64_t expand3(uint64_t x)
-{
-    x = (x | (x << 32)) & 0x1F00000000FFFFull;
-    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
-    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
-    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
-    x = (x | (x << 2)) & 0x1249249249249249ull;
-    return x;
-}
-
-__device__ __forceinline__ uint64_t expand2(uint64_t x)
-{
-    x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
-    x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
-    x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
-    x = (x | (x << 2)) & 0x3333333333333333ull;
-    x = (x | (x << 1)) & 0x5555555555555555ull;
-    return x;
-}
-
-// p01 = (x - pmin) / extent + offset, clamped at 1 - 1e-12 (bbox.py:85-94);
-// coordinate = trunc(p01 * 2^21) clamped to 2^21 - 1 (morton.py:183-185).
-__device__ __forceinline__ uint64_t quantise(double x, double pmin, double extent, double offset)
-{
-    const double top = 1.0 - 1e-12;
-    double p = __dadd_rn(__ddiv_rn(__dsub_rn(x, pmin), extent), offset);
-    p = p > top ? top : p;
-    uint64_t q = __double2ull_rz(__dmul_rn(p, 2097152.0));
-    return q < 2097151ull ? q : 2097151ull;
-}
-
 __global__ void k_morton(const double* __restrict__ pos, int64_t n, int dim,
                          const double* __restrict__ box, uint64_t* __restrict__ keys,
                          int32_t* __restrict__ idx)
@@ -178,14 +147,12 @@ __global__ void k_morton(const double* __restrict__ pos, int64_t n, int dim,
          i += (int64_t)gridDim.x * blockDim.x) {
         uint64_t key;
         if (dim == 3) {
-            uint64_t cx = quantise(pos[3 * i], pmin[0], ext[0], off[0]);
-            uint64_t cy = quantise(pos[3 * i + 1], pmin[1], ext[1], off[1]);
-            uint64_t cz = quantise(pos[3 * i + 2], pmin[2], ext[2], off[2]);
-            key = expand3(cx) | (expand3(cy) << 1) | (expand3(cz) << 2);
+            key = morton3(quantise(pos[3 * i], pmin[0], ext[0], off[0]),
+                          quantise(pos[3 * i + 1], pmin[1], ext[1], off[1]),
+                          quantise(pos[3 * i + 2], pmin[2], ext[2], off[2]));
         } else {
-            uint64_t cx = quantise(pos[2 * i], pmin[0], ext[0], off[0]);
-            uint64_t cy = quantise(pos[2 * i + 1], pmin[1], ext[1], off[1]);
-            key = expand2(cx) | (expand2(cy) << 1);
+            key = morton2(quantise(pos[2 * i], pmin[0], ext[0], off[0]),
+                          quantise(pos[2 * i + 1], pmin[1], ext[1], off[1]));
         }
         keys[i] = key;
         if (idx) idx[i] = (int32_t)i;

@@ -438,7 +438,8 @@ k_traverse_fp32(TreeDev t, FastTree ft, FastArgs a)
         if (valid) {
             const int64_t o = a.out_idx ? a.out_idx[i] : i;
 #pragma unroll
-            for (int k = 0; k < DIM; k++) a.out[o * DIM + k] = __dmul_rn((double)acc[k], conv);
+            for (int k = 0; k < DIM; k++)   // Kahan sum: value = sum - compensation
+                a.out[o * DIM + k] = __dmul_rn(__dsub_rn((double)acc[k], (double)cmp[k]), conv);
         }
     }
 }

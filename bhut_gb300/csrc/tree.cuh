@@ -69,6 +69,49 @@ struct FastTree {
     const float* ndelta; // |com - AABB centre|, normalised, per node (offset criterion)
 };
 
+// Morton encoding (bhut/utils/morton.py:14-45, 183-198) and the quantisation
+// of bhut/space/bbox.py:85-94, shared by the single-tree and batched builds.
+static __device__ __forceinline__ uint64_t expand3(uint64_t x)
+{
+    x = (x | (x << 32)) & 0x1F00000000FFFFull;
+    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+static __device__ __forceinline__ uint64_t expand2(uint64_t x)
+{
+    x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
+    x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
+    x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
+    x = (x | (x << 2)) & 0x3333333333333333ull;
+    x = (x | (x << 1)) & 0x5555555555555555ull;
+    return x;
+}
+
+// p01 = (x - pmin) / extent + offset, clamped at 1 - 1e-12 (bbox.py:85-94);
+// coordinate = trunc(p01 * 2^21) clamped to 2^21 - 1 (morton.py:183-185).
+static __device__ __forceinline__ uint64_t quantise(double x, double pmin, double extent, double offset)
+{
+    const double top = 1.0 - 1e-12;
+    double p = __dadd_rn(__ddiv_rn(__dsub_rn(x, pmin), extent), offset);
+    p = p > top ? top : p;
+    uint64_t q = __double2ull_rz(__dmul_rn(p, 2097152.0));
+    return q < 2097151ull ? q : 2097151ull;
+}
+
+static __device__ __forceinline__ uint64_t morton3(uint64_t cx, uint64_t cy, uint64_t cz)
+{
+    return expand3(cx) | (expand3(cy) << 1) | (expand3(cz) << 2);
+}
+
+static __device__ __forceinline__ uint64_t morton2(uint64_t cx, uint64_t cy)
+{
+    return expand2(cx) | (expand2(cy) << 1);
+}
+
 // Node arrays written by the bottom-up pass.
 struct NodeOut {
     NodeCM* cm;        // (com, mass)

@@ -1,6 +1,7 @@
 """Measurement reports for the engine's forms beyond the plain FP64 path.
 
     python -m bhut_gb300.reports precision [--n 4000000] [--sample 8192]
+    python -m bhut_gb300.reports batched [--nsys 2048]
 
 ``precision``: the galaxy model (70 % exponential disc, 30 % Hernquist bulge,
 equal masses), softening 0.005, theta in {0.3, 0.5, 0.7}.  For each theta the
@@ -87,9 +88,89 @@ def precision_report(n: int = 4_000_000, n_sample: int = 8192, thetas=(0.3, 0.5,
     return lines
 
 
+def batched_report(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: int = 11,
+                   theta: float = 0.5, eps: float = 0.01, G: float = 1.0, reps: int = 3,
+                   plain_sample: int = 64, err_systems: int = 16, criterion: str = "bh"):
+    """``batched``: nsys Plummer spheres (N log-uniform in [nmin, nmax], scale
+    radius uniform in [0.5, 2], own seeds, equal masses 1/N) solved in one
+    batch (FP32 form, CUDA graph, autotuned leaf size and targets per warp);
+    systems/s and accels/s, against the plain per-system GPU path (one
+    single-tree FP64-accurate solve per system) timed on a sample of the
+    systems; errors vs FP64 direct sum on sampled systems."""
+    import torch
+    from . import batch
+    systems = workloads.plummer_batch(nsys, nmin, nmax, seed=seed)
+    pos, m, off = batch.concat_systems(systems)
+    ntot = int(off[-1])
+    _log(f"{nsys} systems, {ntot:,} particles")
+    pd = torch.as_tensor(pos).cuda()
+    md = torch.as_tensor(m).cuda()
+    cfg, times = batch.autotune(pd, md, off, theta=theta, softening=eps, G=G, form="fp32",
+                                criterion=criterion)
+    _log(f"autotune {cfg} {times}")
+    sv = batch.BatchedSolver(leaf_size=cfg["leaf_size"], form="fp32", criterion=criterion,
+                             targets_per_warp=cfg["targets_per_warp"], use_graph=True)
+    sv.load(pd, md, off)
+    out = torch.empty_like(pd)
+    sv.solve(theta=theta, softening=eps, G=G, out=out)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(reps):
+        sv.solve(theta=theta, softening=eps, G=G, out=out)
+    ev1.record()
+    ev1.synchronize()
+    t_batch = ev0.elapsed_time(ev1) / 1e3 / reps
+    p2p, m2p, _ = sv.stats()
+    acc = out.cpu().numpy()
+    sv.close()
+    _log(f"batched solve {t_batch * 1e3:.2f} ms")
+    # plain per-system GPU path (form fast, one Tree per system) on a sample
+    rng = np.random.default_rng(seed + 1)
+    pick = rng.choice(nsys, min(plain_sample, nsys), replace=False)
+    t_plain = 0.0
+    n_plain = 0
+    for s in pick:
+        p_, m_ = systems[s]
+        tr = api.Tree(p_, m_, leaf_size=32, form="fast").build()
+        tr.accelerations(theta=theta, softening=eps, G=G)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tr.rebuild(p_, m_)
+        tr.accelerations(theta=theta, softening=eps, G=G)
+        torch.cuda.synchronize()
+        t_plain += time.perf_counter() - t0
+        n_plain += len(m_)
+        tr.close()
+    plain_sps = len(pick) / t_plain
+    _log(f"plain path: {len(pick)} systems in {t_plain:.3f} s")
+    # accuracy on sampled systems vs FP64 direct sum (all their particles)
+    errs = []
+    for s in rng.choice(nsys, min(err_systems, nsys), replace=False):
+        p_, m_ = systems[s]
+        ref = np.asarray(api.direct_accelerations(p_, m_, softening=eps, G=G))
+        errs.append(precision.error_distribution(acc[off[s]:off[s + 1]], ref))
+    line = {
+        "report": "batched", "workload": f"{nsys} Plummer spheres, N log-uniform in "
+        f"[{nmin}, {nmax}], a ~ U[0.5, 2], own seeds", "particles": ntot, "theta": theta,
+        "softening": eps, "form": "fp32", "criterion": criterion, "config": cfg,
+        "autotune_s": {f"L{k[0]}_tpw{k[1]}": v for k, v in times.items()},
+        "solve_ms": t_batch * 1e3, "systems_per_s": nsys / t_batch,
+        "accels_per_s": ntot / t_batch, "interactions": {"p2p": p2p, "m2p": m2p},
+        "plain_per_system": {"systems_timed": int(len(pick)), "systems_per_s": plain_sps,
+                             "particles": n_plain, "seconds": t_plain},
+        "speedup_systems_per_s": (nsys / t_batch) / plain_sps,
+        "err_vs_direct_median_of_medians": float(np.median([e["median"] for e in errs])),
+        "err_vs_direct_worst_p99": float(max(e["p99"] for e in errs)),
+    }
+    print(json.dumps(line), flush=True)
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("report", choices=["precision"])
+    ap.add_argument("report", choices=["precision", "batched"])
+    ap.add_argument("--nsys", type=int, default=2048)
     ap.add_argument("--n", type=int, default=4_000_000)
     ap.add_argument("--sample", type=int, default=8192)
     ap.add_argument("--criterion", default="bh")
@@ -98,6 +179,8 @@ def main():
     if args.report == "precision":
         precision_report(args.n, args.sample, criterion=args.criterion,
                          thetas=tuple(float(x) for x in args.thetas.split(",")))
+    elif args.report == "batched":
+        batched_report(args.nsys, criterion=args.criterion)
 
 
 if __name__ == "__main__":

@@ -101,6 +101,18 @@ def galaxy(n: int, seed: int = 0, rd: float = 3.0, z0: float = 0.3, a_bulge: flo
     return pos, np.full(n, 1.0 / n)
 
 
+def plummer_batch(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: int = 0,
+                  amin: float = 0.5, amax: float = 2.0):
+    """Independent Plummer spheres: N log-uniform in [nmin, nmax], scale
+    radius uniform in [amin, amax], each with its own seed, equal masses
+    1/N.  Returns a list of (positions, masses)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(nmin), np.log(nmax), nsys)).astype(np.int64)
+    scales = rng.uniform(amin, amax, nsys)
+    seeds = rng.integers(0, 2**31 - 1, nsys)
+    return [plummer(int(n), seed=int(sd), a=float(a)) for n, a, sd in zip(sizes, scales, seeds)]
+
+
 def cube_targets(m: int, seed: int = 0, side: float = 10.0, dim: int = 3) -> np.ndarray:
     """External targets uniform in a centred cube of the given side."""
     rng = np.random.default_rng(seed)

@@ -146,6 +146,39 @@ BHUT_API int bhut_morton_argsort(const double *positions, int64_t n, int dim, ui
 BHUT_API int bhut_morton_argsort_noalloc(const double *positions, int64_t n, int dim,
                                          uint64_t *sorted_keys, int32_t *perm, void *stream);
 
+/* ---- batched form: many independent systems per solve ------------------ */
+/* No counterpart in the reference (which solves one system per call); each
+ * system's result equals a single-system solve with the same form.  Systems
+ * are concatenated: positions (N_total, dim), masses (N_total,), system s
+ * owns particles [offsets[s], offsets[s+1]). */
+typedef struct bhut_batch bhut_batch;
+
+BHUT_API int bhut_batch_create(int dim, int leaf_size, void *stream, bhut_batch **out);
+
+/* form: BHUT_FORM_FP32 (default) or BHUT_FORM_FAST; criterion: BHUT_MAC_*;
+ * targets_per_warp: 32 or 16 (two lanes per target); use_graph: capture the
+ * whole solve (build + traversal) in a CUDA graph and replay it while the
+ * layout, theta, softening, G and output buffer stay the same. */
+BHUT_API int bhut_batch_configure(bhut_batch *b, int form, int criterion, int targets_per_warp,
+                                  int use_graph);
+
+/* Copies the systems in; a new layout (offsets) re-plans node counts, buffers
+ * and the task queue. */
+BHUT_API int bhut_batch_load(bhut_batch *b, const double *positions, const double *masses,
+                             const int64_t *offsets, int64_t nsys);
+
+/* Builds every tree and evaluates all self accelerations; out (N_total, dim)
+ * in input order. */
+BHUT_API int bhut_batch_solve(bhut_batch *b, double theta, double softening, double G, double *out);
+
+BHUT_API int bhut_batch_info(const bhut_batch *b, int64_t *nsys, int64_t *n_total,
+                             int64_t *nodes_total, int64_t *tasks);
+
+/* Pair, monopole and node-visit counts of the last solve. */
+BHUT_API int bhut_batch_stats(const bhut_batch *b, int64_t *p2p, int64_t *m2p, int64_t *visits);
+
+BHUT_API void bhut_batch_destroy(bhut_batch *b);
+
 /* FP64 direct sum (the theta = 0 limit) at m targets, or self accelerations
  * when targets == NULL (then m must equal n). */
 BHUT_API int bhut_direct_accelerations(const double *positions, const double *masses, int64_t n, int dim,

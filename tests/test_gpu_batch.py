@@ -1,0 +1,93 @@
+"""Batched form: many systems per solve, each result identical to solving
+that system alone with the same form."""
+import numpy as np
+import pytest
+
+import bhut_gb300 as bh
+from bhut_gb300 import batch, workloads
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _engine(engine_lib):
+    yield
+
+
+@pytest.fixture(scope="module")
+def systems():
+    return workloads.plummer_batch(nsys=40, nmin=64, nmax=6000, seed=3)
+
+
+def _single(pos, m, form, theta=0.5, eps=0.01, leaf=32):
+    t = bh.Tree(pos, m, leaf_size=leaf, form=form).build()
+    a = t.accelerations(theta=theta, softening=eps)
+    st = t._handle.stats()
+    t.close()
+    return a, st
+
+
+@pytest.mark.parametrize("form", ["fast", "fp32"])
+def test_batch_equals_single_tree(systems, form):
+    pos, m, off = batch.concat_systems(systems)
+    sv = batch.BatchedSolver(form=form, targets_per_warp=32, use_graph=False)
+    sv.load(pos, m, off)
+    acc = sv.solve(theta=0.5, softening=0.01)
+    p2p_tot = 0
+    for s, (p, mm) in enumerate(systems):
+        ref, st = _single(p, mm, form)
+        assert np.array_equal(acc[off[s]:off[s + 1]], ref), s
+        p2p_tot += st[0]
+    assert sv.stats()[0] == p2p_tot
+    sv.close()
+
+
+@pytest.mark.parametrize("form,tol", [("fast", 1e-12), ("fp32", 1e-6)])
+def test_batch_two_lanes_per_target(systems, form, tol):
+    pos, m, off = batch.concat_systems(systems)
+    a32 = batch.BatchedSolver(form=form, targets_per_warp=32, use_graph=False).load(
+        pos, m, off).solve(theta=0.6, softening=0.02)
+    sv = batch.BatchedSolver(form=form, targets_per_warp=16, use_graph=False)
+    a16 = sv.load(pos, m, off).solve(theta=0.6, softening=0.02)
+    assert rel_l2(a16, a32) < tol
+    sv.close()
+
+
+def test_graph_replay_and_reload(systems):
+    import torch
+    pos, m, off = batch.concat_systems(systems)
+    pd, md = torch.from_numpy(pos).cuda(), torch.from_numpy(m).cuda()
+    sv = batch.BatchedSolver(form="fp32", use_graph=True)
+    sv.load(pd, md, off)
+    out = torch.empty_like(pd)
+    a1 = sv.solve(theta=0.5, softening=0.01, out=out).clone()
+    a2 = sv.solve(theta=0.5, softening=0.01, out=out).clone()
+    assert torch.equal(a1, a2)
+    moved = pd * 1.01 + 0.001
+    sv.load(moved, md, off)                 # same layout: the graph is replayed
+    a3 = sv.solve(theta=0.5, softening=0.01, out=out).cpu().numpy()
+    ref = batch.BatchedSolver(form="fp32", use_graph=False).load(
+        moved.cpu().numpy(), m, off).solve(theta=0.5, softening=0.01)
+    assert np.array_equal(a3, ref)
+    sv.close()
+
+
+def test_batch_fast_form_against_oracle(systems, oracle_mod):
+    accs = batch.batched_accelerations(systems[:6], theta=0.5, softening=0.01, form="fast")
+    for (p, mm), a in zip(systems[:6], accs):
+        ot = oracle_mod.build_tree(p, mm, 32)
+        ref = oracle_mod.accelerations(ot, p, mm, theta=0.5, softening=0.01)
+        assert rel_l2(a, ref) <= 1e-11
+
+
+def test_batch_2d_and_errors():
+    sys2 = [workloads.gaussian(n, seed=n, dim=2) for n in (100, 700, 33)]
+    accs = batch.batched_accelerations(sys2, theta=0.5, softening=0.02, form="fp32")
+    for (p, mm), a in zip(sys2, accs):
+        ref = bh.accelerations(p, mm, dim=2, form="fp32", theta=0.5, softening=0.02)
+        assert np.array_equal(a, ref)
+    with pytest.raises(ValueError):
+        batch.BatchedSolver(form="exact")
+    with pytest.raises(ValueError):
+        batch.BatchedSolver(form="fast", criterion="bh_offset")
