@@ -64,7 +64,10 @@ SIGNATURES = {
     "bhut_batch_solve": (_INT, [_VP, _D, _D, _D, _VP]),
     "bhut_batch_info": (_INT, [_VP] + [ctypes.POINTER(_I64)] * 4),
     "bhut_batch_stats": (_INT, [_VP] + [ctypes.POINTER(_I64)] * 3),
+    "bhut_batch_keep_order": (_INT, [_VP, _VP, _VP]),
+    "bhut_batch_order": (_INT, [_VP, _VP]),
     "bhut_batch_destroy": (None, [_VP]),
+    "bhut_leapfrog": (_INT, [_VP, _VP, _VP, _I64, _INT, _D, _D, _VP]),
 }
 
 _lock = threading.Lock()

@@ -132,6 +132,29 @@ __global__ void k_seg_key2(const int32_t* __restrict__ perm, const int32_t* __re
         key2[i] = (uint64_t)sys_of[perm[i]];
 }
 
+// Systems marked in `keep` reuse the permutation given by the caller (a
+// refit: their Morton order and topology are frozen, node boxes and moments
+// are recomputed from the new positions); the others keep the fresh sort.
+__global__ void k_seg_keep_perm(const int64_t* __restrict__ off, const uint8_t* __restrict__ keep,
+                                const int32_t* __restrict__ perm_in, int32_t* __restrict__ perm)
+{
+    const int s = blockIdx.x;
+    if (!keep[s]) return;
+    for (int64_t i = off[s] + threadIdx.x; i < off[s + 1]; i += blockDim.x) perm[i] = perm_in[i];
+}
+
+// Leapfrog kick and drift: v += kick * a, then x += drift * v.
+__global__ void k_leapfrog(double* __restrict__ pos, double* __restrict__ vel,
+                           const double* __restrict__ acc, int64_t n, double kick, double drift)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = __fma_rn(kick, acc[i], vel[i]);
+        vel[i] = v;
+        if (drift != 0.0) pos[i] = __fma_rn(drift, v, pos[i]);
+    }
+}
+
 // One block per system.  Thread 0 builds the per-depth tables of the
 // closed form (see k_topology in build.cu) in shared memory; the block then
 // walks that system's BFS slots.
@@ -501,7 +524,8 @@ struct bhut_batch {
     BufB pos, mass, d_part_off, d_node_off, d_leaf_off, d_tasks, keys, perm, sys_of, key2,
         sx, sy, sz, sm, cm, size, center, half, lo, hi, first_child, start, count, parent,
         leaf_list, arrive, sort_scratch, box, frames, ph, pl, nh, nl, nsize, ndelta, counter,
-        err, stats, out;
+        err, stats, out, keep, perm_in;
+    bool keep_active = false;
     unsigned long long last_stats[5] = {0, 0, 0, 0, 0};
     cudaGraphExec_t graph = nullptr;
     bool use_graph = false;
@@ -512,7 +536,7 @@ struct bhut_batch {
                      &sys_of, &key2, &sx, &sy, &sz, &sm, &cm, &size, &center, &half, &lo, &hi,
                      &first_child, &start, &count, &parent, &leaf_list, &arrive, &sort_scratch,
                      &box, &frames, &ph, &pl, &nh, &nl, &nsize, &ndelta, &counter, &err, &stats,
-                     &out, nullptr};
+                     &out, &keep, &perm_in, nullptr};
 
     TreeDev dev() const
     {
@@ -622,6 +646,9 @@ int plan_layout(bhut_batch* b, const int64_t* offsets, int64_t nsys)
     BHUT_TRY(b->err.ensure(sizeof(unsigned), s));
     BHUT_TRY(b->stats.ensure(sizeof(unsigned long long) * 8, s));
     BHUT_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(unsigned), s));
+    BHUT_TRY(b->keep.ensure(nsys, s));
+    BHUT_TRY(b->perm_in.ensure(sizeof(int32_t) * ntot, s));
+    b->keep_active = false;
     b->layout_valid = true;
     b->topo_valid = false;
     drop_graph(b);
@@ -661,6 +688,14 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
         note_launches(1);
         BHUT_TRY(radix_sort_pairs(b->key2.as<uint64_t>(), b->perm.as<int32_t>(), n,
                                   bits_for(ns - 1), b->sort_scratch.p, s));
+    }
+    if (b->keep_active) {
+        k_seg_keep_perm<<<(unsigned)ns, kSegThreads, 0, s>>>(b->d_part_off.as<int64_t>(),
+                                                           b->keep.as<uint8_t>(),
+                                                           b->perm_in.as<int32_t>(),
+                                                           b->perm.as<int32_t>());
+        BHUT_CUDA(cudaGetLastError());
+        note_launches(1);
     }
     BHUT_TRY(launch_gather(b->pos.as<double>(), b->mass.as<double>(), b->perm.as<int32_t>(), n,
                            dim, b->sx.as<double>(), b->sy.as<double>(), b->sz.as<double>(),
@@ -840,6 +875,55 @@ int bhut_batch_solve(bhut_batch* b, double theta, double softening, double G, do
         BHUT_CUDA(cudaMemcpyAsync(out, dst, sizeof(double) * b->ntot * b->dim,
                                   cudaMemcpyDeviceToHost, b->stream));
     return check_batch_err(b);
+}
+
+int bhut_batch_keep_order(bhut_batch* b, const uint8_t* keep, const int32_t* perm)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (!b->layout_valid) { set_error("load systems first"); return kNotBuilt; }
+    cudaStream_t s = b->stream;
+    if (!keep) {
+        if (b->keep_active) drop_graph(b);
+        b->keep_active = false;
+        return kOk;
+    }
+    if (!perm) { set_error("perm is NULL"); return kInvalid; }
+    BHUT_CUDA(cudaMemcpyAsync(b->keep.p, keep, b->nsys, is_device_pointer(keep)
+                              ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    BHUT_CUDA(cudaMemcpyAsync(b->perm_in.p, perm, sizeof(int32_t) * b->ntot,
+                              is_device_pointer(perm) ? cudaMemcpyDeviceToDevice
+                                                      : cudaMemcpyHostToDevice, s));
+    if (!b->keep_active) drop_graph(b);
+    b->keep_active = true;
+    return kOk;
+}
+
+int bhut_batch_order(const bhut_batch* b, int32_t* perm)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (!b->layout_valid || !perm) { set_error("nothing to copy"); return kInvalid; }
+    BHUT_CUDA(cudaMemcpyAsync(perm, b->perm.p, sizeof(int32_t) * b->ntot, cudaMemcpyDefault,
+                              b->stream));
+    BHUT_CUDA(cudaStreamSynchronize(b->stream));
+    return kOk;
+}
+
+int bhut_leapfrog(double* positions, double* velocities, const double* accelerations, int64_t n,
+                  int dim, double kick, double drift, void* stream)
+{
+    if (n <= 0) return kOk;
+    if (dim != 2 && dim != 3) { set_error("dim must be 2 or 3, got %d", dim); return kInvalid; }
+    if (!is_device_pointer(positions) || !is_device_pointer(velocities) ||
+        !is_device_pointer(accelerations)) {
+        set_error("bhut_leapfrog needs device pointers");
+        return kInvalid;
+    }
+    const int64_t m = n * dim;
+    k_leapfrog<<<grid_for(m, 256), 256, 0, (cudaStream_t)stream>>>(positions, velocities,
+                                                                   accelerations, m, kick, drift);
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
+    return kOk;
 }
 
 int bhut_batch_info(const bhut_batch* b, int64_t* nsys, int64_t* n_total, int64_t* nodes_total,

@@ -2,6 +2,7 @@
 
     python -m bhut_gb300.reports precision [--n 4000000] [--sample 8192]
     python -m bhut_gb300.reports batched [--nsys 2048]
+    python -m bhut_gb300.reports served [--count 24]
 
 ``precision``: the galaxy model (70 % exponential disc, 30 % Hernquist bulge,
 equal masses), softening 0.005, theta in {0.3, 0.5, 0.7}.  For each theta the
@@ -167,9 +168,55 @@ def batched_report(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: i
     return line
 
 
+def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: int = 21,
+                  plain_seconds: float = 90.0, err_requests: int = 4):
+    """``served``: a Poisson stream (mean ``rate`` requests/s) of ``count``
+    systems (N log-uniform in [1e3, 2e6], half Plummer, half uniform cubes of
+    side 2, velocities N(0, 0.1^2)), each advanced ``steps`` KDK steps
+    (dt = 1e-3, theta = 0.5, eps = 0.01), refit every step, rebuild every 10;
+    the continuous-batching server (FP32 form, offset criterion) against the
+    plain per-request path (form fast, reference criterion), both in real
+    time from the same arrival schedule; latencies include queueing.  Errors
+    vs FP64 direct sum on the initial conditions of a few requests."""
+    from . import serve
+    reqs = serve.request_stream(count, rate=rate, steps=steps, seed=seed)
+    total_n = sum(r.n for r in reqs)
+    _log(f"{count} requests, {total_n:,} particles, offered "
+         f"{rate * steps * total_n / count:.3g} accels/s")
+    # accuracy of both configurations on initial conditions
+    errs_srv, errs_plain = [], []
+    for r in sorted(reqs, key=lambda r: r.n)[:err_requests]:
+        idx = precision.sample_indices(r.n, 2048, seed=1)
+        ref = precision.direct_reference(r.positions, r.masses, idx, softening=0.01)
+        a_s = api.accelerations(r.positions, r.masses, theta=0.5, softening=0.01,
+                                form="fp32", criterion="bh_offset")
+        a_p = api.accelerations(r.positions, r.masses, theta=0.5, softening=0.01, form="fast")
+        errs_srv.append(precision.error_distribution(a_s[idx], ref)["median"])
+        errs_plain.append(precision.error_distribution(a_p[idx], ref)["median"])
+    _log(f"median errors: served {errs_srv}, plain {errs_plain}")
+    sv = serve.Server(theta=0.5, softening=0.01, dt=1e-3, rebuild_every=10, form="fp32",
+                      criterion="bh_offset")
+    st = sv.run(reqs, realtime=True)
+    sv.close()
+    _log(f"served: {st}")
+    reqs2 = serve.request_stream(count, rate=rate, steps=steps, seed=seed)
+    pl = serve.plain_path(reqs2, theta=0.5, softening=0.01, dt=1e-3, rebuild_every=10,
+                          realtime=True, max_seconds=plain_seconds)
+    _log(f"plain: {pl}")
+    line = {"report": "served", "requests": count, "rate_per_s": rate, "steps": steps,
+            "particles": total_n, "served": st, "plain": pl,
+            "solves_per_s_ratio": st["solves_per_s"] / pl["solves_per_s"]
+            if pl["solves_per_s"] else None,
+            "median_err_vs_direct": {"served_fp32_offset": float(np.median(errs_srv)),
+                                     "plain_fast_bh": float(np.median(errs_plain))}}
+    print(json.dumps(line), flush=True)
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("report", choices=["precision", "batched"])
+    ap.add_argument("report", choices=["precision", "batched", "served"])
+    ap.add_argument("--count", type=int, default=24)
     ap.add_argument("--nsys", type=int, default=2048)
     ap.add_argument("--n", type=int, default=4_000_000)
     ap.add_argument("--sample", type=int, default=8192)
@@ -181,6 +228,8 @@ def main():
                          thetas=tuple(float(x) for x in args.thetas.split(",")))
     elif args.report == "batched":
         batched_report(args.nsys, criterion=args.criterion)
+    elif args.report == "served":
+        served_report(args.count)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,304 @@
+"""Served form: continuous batching of N-body systems with device-resident state.
+
+A request is one N-body system (positions, velocities, masses) to advance by
+``steps`` kick-drift-kick leapfrog steps.  The server keeps every admitted
+system's state in HBM and advances all of them together, one batched solve
+per tick:
+
+* admission: a queued request is admitted at a tick boundary once it has
+  arrived and its estimated device footprint fits the HBM budget (and the
+  optional cap on resident particles);
+* each tick: first half-kick and drift (``bhut_leapfrog``), one batched
+  solve of every resident system (``bhut_batch_*``), second half-kick;
+* each system refits its tree on its own schedule -- its Morton order is kept
+  (``bhut_batch_keep_order``) and node boxes and moments are recomputed --
+  and rebuilds it every ``rebuild_every`` of its own steps.  Nothing a system
+  computes depends on which other systems share the batch, so a request's
+  trajectory is the same alone and in any mix (bit for bit);
+* a finished request leaves at the next tick boundary and frees its slot;
+* latency = completion time - arrival time (queueing included).
+
+``plain_path`` runs the same stream the simple way for comparison: one
+request at a time, one ``Tree`` per request (form ``fast``), ``refit`` every
+step and ``rebuild`` every ``rebuild_every`` steps.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib, api, workloads
+from .batch import BatchedSolver
+
+# Device bytes per resident particle: request state (x, v, a, m, order),
+# the batch's copies, sort scratch and float-float particles, and the node
+# arrays (about 2 N / leaf_size nodes of ~190 B).
+STATE_BYTES = 3 * 24 + 8 + 4
+BATCH_BYTES = 24 + 8 + 8 + 8 + 4 + 4 + 32 + 32 + 12 + 4 + 24
+NODE_BYTES = 190
+
+
+def bytes_per_particle(leaf_size: int) -> float:
+    return STATE_BYTES + BATCH_BYTES + 2.0 * NODE_BYTES / leaf_size
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float
+    positions: np.ndarray
+    velocities: np.ndarray
+    masses: np.ndarray
+    steps: int = 100
+    kind: str = ""
+    # runtime state
+    steps_done: int = 0
+    solves: int = 0
+    primed: bool = False
+    admitted_at: float | None = None
+    done_at: float | None = None
+    order: object = None          # local Morton order of the last solve (device int32)
+    slot: tuple = field(default=(0, 0))
+    acc: object = None
+
+    @property
+    def n(self) -> int:
+        return len(self.masses)
+
+    @property
+    def latency(self) -> float | None:
+        return None if self.done_at is None else self.done_at - self.arrival
+
+
+def request_stream(count: int, *, rate: float = 200.0, nmin: int = 1000, nmax: int = 2_000_000,
+                   steps: int = 100, seed: int = 0, vel_sigma: float = 0.1) -> list[Request]:
+    """Poisson arrivals (mean ``rate`` per second); N log-uniform in
+    [nmin, nmax]; half Plummer spheres (a = 1), half uniform cubes of side 2;
+    equal masses 1/N; velocities N(0, vel_sigma^2) per component."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, count))
+    out = []
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))
+        sd = int(rng.integers(0, 2**31 - 1))
+        if rng.random() < 0.5:
+            pos, m = workloads.plummer(n, seed=sd)
+            kind = "plummer"
+        else:
+            pos, m = workloads.uniform_cube(n, seed=sd, side=2.0)
+            kind = "cube"
+        vel = np.random.default_rng(sd + 1).normal(0.0, vel_sigma, (n, 3))
+        out.append(Request(i, float(t[i]), pos, vel, m, steps=steps, kind=kind))
+    return out
+
+
+def _leapfrog(L, pos, vel, acc, n, kick, drift, stream):
+    _lib.check(L.bhut_leapfrog(pos.data_ptr(), vel.data_ptr(), acc.data_ptr(), int(n), 3,
+                               float(kick), float(drift), stream))
+
+
+class Server:
+    """Continuous-batching server; see the module docstring."""
+
+    def __init__(self, *, theta: float = 0.5, softening: float = 0.01, G: float = 1.0,
+                 dt: float = 1e-3, rebuild_every: int = 10, form: str = "fp32",
+                 criterion: str = "bh_offset", leaf_size: int = 16, targets_per_warp: int = 32,
+                 hbm_budget: float = 150e9, max_active_particles: int | None = None):
+        import torch
+        self.torch = torch
+        self.theta, self.eps, self.G, self.dt = theta, softening, G, dt
+        self.rebuild_every = rebuild_every
+        self.leaf_size = leaf_size
+        self.hbm_budget = hbm_budget
+        self.max_active = max_active_particles
+        self.L = _lib.load()
+        self.stream = torch.cuda.current_stream().cuda_stream
+        self.solver = BatchedSolver(dim=3, leaf_size=leaf_size, form=form, criterion=criterion,
+                                    targets_per_warp=targets_per_warp, use_graph=False,
+                                    stream=self.stream)
+        self.active: list[Request] = []
+        self.finished: list[Request] = []
+        self.ticks = 0
+        self.solves = 0
+        self.accels = 0
+        self.peak_bytes = 0.0
+
+    # -- device state ------------------------------------------------------
+    def _fits(self, r: Request) -> bool:
+        resident = sum(a.n for a in self.active)
+        if self.max_active is not None and self.active and resident + r.n > self.max_active:
+            return False
+        return (resident + r.n) * bytes_per_particle(self.leaf_size) <= self.hbm_budget
+
+    def _pack(self):
+        """Concatenates the resident systems' state into one set of device
+        arrays (after an admission or a retirement)."""
+        torch = self.torch
+        dev = "cuda"
+        parts_x, parts_v, parts_a, parts_m = [], [], [], []
+        for r in self.active:
+            parts_x.append(r.positions)
+            parts_v.append(r.velocities)
+            parts_a.append(r.acc)
+            parts_m.append(r.masses)
+        self.x = torch.cat(parts_x).contiguous()
+        self.v = torch.cat(parts_v).contiguous()
+        self.a = torch.cat(parts_a).contiguous()
+        self.m = torch.cat(parts_m).contiguous()
+        sizes = [r.n for r in self.active]
+        self.off = np.zeros(len(sizes) + 1, dtype=np.int64)
+        self.off[1:] = np.cumsum(sizes)
+        for k, r in enumerate(self.active):          # views into the packed arrays
+            s, e = int(self.off[k]), int(self.off[k + 1])
+            r.positions, r.velocities, r.acc, r.masses = self.x[s:e], self.v[s:e], self.a[s:e], \
+                self.m[s:e]
+            r.slot = (s, e)
+        self.perm = torch.empty(int(self.off[-1]), dtype=torch.int32, device=dev)
+        self.peak_bytes = max(self.peak_bytes,
+                              float(self.off[-1]) * bytes_per_particle(self.leaf_size))
+
+    # -- one tick ------------------------------------------------------------
+    def tick(self) -> None:
+        torch = self.torch
+        dt = self.dt
+        for r in self.active:                       # first half-kick + drift
+            if r.primed:
+                _leapfrog(self.L, r.positions, r.velocities, r.acc, r.n, 0.5 * dt, dt,
+                          self.stream)
+        keep = np.zeros(len(self.active), dtype=np.uint8)
+        perm_in = None
+        for k, r in enumerate(self.active):         # refit unless a rebuild is due
+            if r.order is not None and r.primed and r.steps_done % self.rebuild_every != 0:
+                keep[k] = 1
+        if keep.any():
+            perm_in = torch.cat([
+                (r.order + int(self.off[k])) if r.order is not None
+                else torch.zeros(r.n, dtype=torch.int32, device="cuda")
+                for k, r in enumerate(self.active)])
+            self.solver.load(self.x, self.m, self.off)
+            _lib.check(self.L.bhut_batch_keep_order(self.solver.h, keep.ctypes.data,
+                                                    perm_in.data_ptr()))
+        else:
+            self.solver.load(self.x, self.m, self.off)
+            _lib.check(self.L.bhut_batch_keep_order(self.solver.h, None, None))
+        self.solver.solve(theta=self.theta, softening=self.eps, G=self.G, out=self.a)
+        _lib.check(self.L.bhut_batch_order(self.solver.h, self.perm.data_ptr()))
+        for k, r in enumerate(self.active):
+            s, e = r.slot
+            r.order = self.perm[s:e] - s
+            if r.primed:                            # second half-kick
+                _leapfrog(self.L, r.positions, r.velocities, r.acc, r.n, 0.5 * dt, 0.0,
+                          self.stream)
+                r.steps_done += 1
+            else:
+                r.primed = True                     # a(0): the initial force evaluation
+            r.solves += 1
+        self.solves += len(self.active)
+        self.accels += int(self.off[-1])
+        self.ticks += 1
+
+    # -- the loop ----------------------------------------------------------
+    def run(self, requests: list[Request], *, realtime: bool = True,
+            max_seconds: float | None = None) -> dict:
+        torch = self.torch
+        queue = sorted(requests, key=lambda r: r.arrival)
+        t_start = time.perf_counter()
+
+        def now():
+            return time.perf_counter() - t_start
+
+        changed = False
+        while queue or self.active:
+            t = now()
+            if max_seconds is not None and t > max_seconds:
+                break
+            while queue and (queue[0].arrival <= t or not realtime) and self._fits(queue[0]):
+                r = queue.pop(0)
+                r.admitted_at = t
+                r.positions = torch.as_tensor(np.asarray(r.positions), device="cuda").clone()
+                r.velocities = torch.as_tensor(np.asarray(r.velocities), device="cuda").clone()
+                r.masses = torch.as_tensor(np.asarray(r.masses), device="cuda").clone()
+                r.acc = torch.zeros_like(r.positions)
+                self.active.append(r)
+                changed = True
+            if not self.active:
+                if queue and realtime:
+                    time.sleep(max(0.0, min(queue[0].arrival - t, 0.05)))
+                continue
+            if changed:
+                self._pack()
+                changed = False
+            self.tick()
+            torch.cuda.current_stream().synchronize()
+            t = now()
+            done = [r for r in self.active if r.steps_done >= r.steps]
+            if done:
+                for r in done:
+                    r.done_at = t
+                    self.active.remove(r)
+                    self.finished.append(r)
+                    r.final_positions = r.positions.clone()
+                    r.final_velocities = r.velocities.clone()
+                changed = bool(self.active)
+        wall = now()
+        lat = np.array([r.latency for r in self.finished if r.latency is not None])
+        return {
+            "requests_done": len(self.finished), "wall_s": wall, "ticks": self.ticks,
+            "solves": self.solves, "solves_per_s": self.solves / wall if wall else 0.0,
+            "accels_per_s": self.accels / wall if wall else 0.0,
+            "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else None,
+            "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None,
+            "peak_resident_bytes_est": self.peak_bytes,
+        }
+
+    def close(self):
+        self.solver.close()
+
+
+def plain_path(requests: list[Request], *, theta: float = 0.5, softening: float = 0.01,
+               G: float = 1.0, dt: float = 1e-3, rebuild_every: int = 10, form: str = "fast",
+               leaf_size: int = 32, realtime: bool = True, max_seconds: float | None = None) -> dict:
+    """The same stream, one request at a time through the public Tree API."""
+    import torch
+    queue = sorted(requests, key=lambda r: r.arrival)
+    L = _lib.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    t_start = time.perf_counter()
+    solves = 0
+    accels = 0
+    done = []
+    for r in queue:
+        t = time.perf_counter() - t_start
+        if max_seconds is not None and t > max_seconds:
+            break
+        if realtime and r.arrival > t:
+            time.sleep(r.arrival - t)
+        x = torch.as_tensor(np.asarray(r.positions), device="cuda").clone()
+        v = torch.as_tensor(np.asarray(r.velocities), device="cuda").clone()
+        m = torch.as_tensor(np.asarray(r.masses), device="cuda").clone()
+        tree = api.Tree(x, m, leaf_size=leaf_size, form=form).build()
+        a = tree.accelerations(theta=theta, softening=softening, G=G)
+        solves += 1
+        for step in range(r.steps):
+            _leapfrog(L, x, v, a, r.n, 0.5 * dt, dt, stream)
+            if (step + 1) % rebuild_every == 0:
+                tree.rebuild(x, m)
+            else:
+                tree.refit(x, m)
+            a = tree.accelerations(theta=theta, softening=softening, G=G)
+            _leapfrog(L, x, v, a, r.n, 0.5 * dt, 0.0, stream)
+            solves += 1
+        torch.cuda.synchronize()
+        accels += r.n * (r.steps + 1)
+        tree.close()
+        r.done_at = time.perf_counter() - t_start
+        done.append(r)
+    wall = time.perf_counter() - t_start
+    lat = np.array([r.done_at - r.arrival for r in done])
+    return {"requests_done": len(done), "wall_s": wall, "solves": solves,
+            "solves_per_s": solves / wall if wall else 0.0,
+            "accels_per_s": accels / wall if wall else 0.0,
+            "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else None,
+            "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None}

@@ -177,7 +177,23 @@ BHUT_API int bhut_batch_info(const bhut_batch *b, int64_t *nsys, int64_t *n_tota
 /* Pair, monopole and node-visit counts of the last solve. */
 BHUT_API int bhut_batch_stats(const bhut_batch *b, int64_t *p2p, int64_t *m2p, int64_t *visits);
 
+/* Refit instead of rebuild for chosen systems: for every s with keep[s] != 0
+ * the next solves reuse the Morton order of `perm` (global indices, the
+ * layout of the last load) instead of sorting; node boxes, masses and
+ * centres of mass are recomputed from the current positions, the topology
+ * is unchanged.  keep == NULL returns to a full rebuild of every system. */
+BHUT_API int bhut_batch_keep_order(bhut_batch *b, const uint8_t *keep, const int32_t *perm);
+
+/* Copies the permutation of the last solve (global indices) to perm. */
+BHUT_API int bhut_batch_order(const bhut_batch *b, int32_t *perm);
+
 BHUT_API void bhut_batch_destroy(bhut_batch *b);
+
+/* Leapfrog update on device arrays (n, dim): v += kick * a, then, when
+ * drift != 0, x += drift * v.  A kick-drift-kick step is
+ * (kick = dt/2, drift = dt), a new acceleration, then (kick = dt/2, drift = 0). */
+BHUT_API int bhut_leapfrog(double *positions, double *velocities, const double *accelerations,
+                           int64_t n, int dim, double kick, double drift, void *stream);
 
 /* FP64 direct sum (the theta = 0 limit) at m targets, or self accelerations
  * when targets == NULL (then m must equal n). */
