@@ -28,6 +28,7 @@ FORMS = {"exact": FORM_EXACT, "fast": FORM_FAST, "fp32": FORM_FP32}
 MAC_BH = 0
 MAC_OFFSET = 1
 CRITERIA = {"bh": MAC_BH, "bh_offset": MAC_OFFSET}
+MULTIPOLES = {"mono": 0, "quad": 1}
 
 _VP = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -46,6 +47,7 @@ SIGNATURES = {
     "bhut_tree_accel_targets": (_INT, [_VP, _VP, _I64, _D, _D, _D, _VP]),
     "bhut_tree_set_form": (_INT, [_VP, _INT]),
     "bhut_tree_set_criterion": (_INT, [_VP, _INT]),
+    "bhut_tree_set_multipole": (_INT, [_VP, _INT]),
     "bhut_tree_info": (_INT, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                               ctypes.POINTER(_INT), ctypes.POINTER(_INT)]),
     "bhut_tree_export": (_INT, [_VP] * 11),
@@ -60,6 +62,7 @@ SIGNATURES = {
     "bhut_morton_argsort_noalloc": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),
     "bhut_batch_create": (_INT, [_INT, _INT, _VP, ctypes.POINTER(_VP)]),
     "bhut_batch_configure": (_INT, [_VP, _INT, _INT, _INT, _INT]),
+    "bhut_batch_set_multipole": (_INT, [_VP, _INT]),
     "bhut_batch_load": (_INT, [_VP, _VP, _VP, _VP, _I64]),
     "bhut_batch_solve": (_INT, [_VP, _D, _D, _D, _VP]),
     "bhut_batch_info": (_INT, [_VP] + [ctypes.POINTER(_I64)] * 4),

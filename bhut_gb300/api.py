@@ -12,7 +12,9 @@ arithmetic -- ``"exact"`` (FP64; pair terms bit-identical to the reference's
 Numba loop), ``"fast"`` (FP64-accurate float-float arithmetic on the FP32
 pipe) or ``"fp32"`` (the FP32/Kahan precision form).  ``criterion`` accepts,
 besides the reference's ``"bh"``, ``"bh_offset"`` (open when
-|x - com| < size/theta + |com - box centre|), available with ``form="fp32"``.
+|x - com| < size/theta + |com - box centre|), available with ``form="fp32"``;
+``multipole`` accepts, besides ``"mono"``, ``"quad"`` (monopole plus traceless
+quadrupole per node), also with ``form="fp32"`` only.
 """
 from __future__ import annotations
 
@@ -169,6 +171,15 @@ def _criterion_code(criterion: str, form: str) -> int:
     return _lib.CRITERIA[criterion]
 
 
+def _multipole_code(multipole: str, form: str) -> int:
+    if multipole not in _lib.MULTIPOLES:
+        raise ValueError(f"multipole must be 'mono', got '{multipole}'")
+    if multipole != "mono" and form != "fp32":
+        raise ValueError(f"multipole must be 'mono', got '{multipole}' "
+                         "(form='fp32' also accepts 'quad')")
+    return _lib.MULTIPOLES[multipole]
+
+
 # ---------------------------------------------------------------------------
 # TreeData export (bhut/tree/node.py:15-77)
 # ---------------------------------------------------------------------------
@@ -228,9 +239,10 @@ class _Handle:
         except Exception:
             pass
 
-    def set_form(self, form: str, criterion: str = "bh") -> None:
+    def set_form(self, form: str, criterion: str = "bh", multipole: str = "mono") -> None:
         _lib.check(self.L.bhut_tree_set_form(self.h, _form_code(form)))
         _lib.check(self.L.bhut_tree_set_criterion(self.h, _criterion_code(criterion, form)))
+        _lib.check(self.L.bhut_tree_set_multipole(self.h, _multipole_code(multipole, form)))
 
     def build(self, pos, m) -> None:
         _sync_torch(pos, m)
@@ -324,9 +336,10 @@ def accelerations(
     """
     if criterion not in _lib.CRITERIA:
         raise ValueError(f"criterion must be 'bh', got '{criterion}'")
-    if multipole != "mono":
+    if multipole not in _lib.MULTIPOLES:
         raise ValueError(f"multipole must be 'mono', got '{multipole}'")
     _criterion_code(criterion, form or DEFAULT_FORM)
+    _multipole_code(multipole, form or DEFAULT_FORM)
     _check_backend(positions, backend)
     positions, masses, softening = _validate_accelerations_inputs(
         positions, masses, dim=dim, softening=softening, theta=theta, G=G, leaf_size=leaf_size)
@@ -338,7 +351,7 @@ def accelerations(
         raise ValueError("Opening angle theta must be non-negative")
     h = _Handle(dim, leaf_size)
     try:
-        h.set_form(form or DEFAULT_FORM, criterion)
+        h.set_form(form or DEFAULT_FORM, criterion, multipole)
         h.build(positions, masses)
         out = _empty_like_out(positions, (n, dim))
         h.accel_self(theta, eps, G, out)
@@ -372,7 +385,8 @@ class Tree:
     """
 
     def __init__(self, positions, masses, *, leaf_size: int = 32, backend: str = "auto",
-                 dim: int = 3, form: str | None = None, criterion: str = "bh"):
+                 dim: int = 3, form: str | None = None, criterion: str = "bh",
+                 multipole: str = "mono"):
         _validate_dimensions(dim)
         self.positions, self.masses, _ = _validate_accelerations_inputs(
             positions, masses, dim=dim, softening=0.0, theta=0.5, G=1.0, leaf_size=leaf_size)
@@ -386,6 +400,8 @@ class Tree:
         _form_code(self._form)
         self._criterion = criterion
         _criterion_code(criterion, self._form)
+        self._multipole = multipole
+        _multipole_code(multipole, self._form)
         _check_backend(self.positions, backend)
 
     # -- reference attribute ``_tree``: None until built --------------------
@@ -413,13 +429,16 @@ class Tree:
         self._is_built = False
         self._tree_cache = None
 
-    def set_form(self, form: str, criterion: str = "bh") -> "Tree":
+    def set_form(self, form: str, criterion: str = "bh", multipole: str = "mono") -> "Tree":
         """Traversal arithmetic ("exact", "fast", "fp32") and, for "fp32",
-        the opening criterion ("bh" or "bh_offset")."""
+        the opening criterion ("bh" or "bh_offset") and node expansion
+        ("mono" or "quad")."""
         _form_code(form)
         _criterion_code(criterion, form)
+        _multipole_code(multipole, form)
         self._form = form
         self._criterion = criterion
+        self._multipole = multipole
         return self
 
     def build(self) -> "Tree":
@@ -491,7 +510,7 @@ class Tree:
             raise ValueError(f"theta must be non-negative, got {theta}")
         out = _empty_like_out(targets, (M, self.dim))
         if M:
-            self._handle.set_form(self._form, self._criterion)
+            self._handle.set_form(self._form, self._criterion, self._multipole)
             self._handle.accel_targets(targets, theta, eps, G, out)
         return out
 
@@ -507,7 +526,7 @@ class Tree:
             raise ValueError("Opening angle theta must be non-negative")
         n = _shape(self.positions)[0]
         out = _empty_like_out(self.positions, (n, self.dim))
-        self._handle.set_form(self._form, self._criterion)
+        self._handle.set_form(self._form, self._criterion, self._multipole)
         self._handle.accel_self(theta, float(softening), G, out)
         return out
 

@@ -33,7 +33,7 @@ class BatchedSolver:
 
     def __init__(self, *, dim: int = 3, leaf_size: int = 32, form: str = "fp32",
                  criterion: str = "bh", targets_per_warp: int = 32, use_graph: bool = True,
-                 stream: int | None = None):
+                 stream: int | None = None, multipole: str = "mono"):
         self.L = _lib.load()
         self.dim = dim
         self.leaf_size = leaf_size
@@ -41,19 +41,25 @@ class BatchedSolver:
         _lib.check(self.L.bhut_batch_create(int(dim), int(leaf_size), stream, ctypes.byref(h)))
         self.h = h
         self.configure(form=form, criterion=criterion, targets_per_warp=targets_per_warp,
-                       use_graph=use_graph)
+                       use_graph=use_graph, multipole=multipole)
         self.offsets = None
         self._keep = None
 
     def configure(self, *, form: str = "fp32", criterion: str = "bh", targets_per_warp: int = 32,
-                  use_graph: bool = True) -> None:
+                  use_graph: bool = True, multipole: str = "mono") -> None:
         if form not in ("fp32", "fast"):
             raise ValueError(f"the batched solver runs form 'fp32' or 'fast', got {form!r}")
         if criterion not in _lib.CRITERIA:
             raise ValueError(f"criterion must be 'bh', got '{criterion}'")
         _lib.check(self.L.bhut_batch_configure(self.h, _lib.FORMS[form], _lib.CRITERIA[criterion],
                                                int(targets_per_warp), int(bool(use_graph))))
-        self.form, self.criterion = form, criterion
+        if multipole not in _lib.MULTIPOLES:
+            raise ValueError(f"multipole must be 'mono', got '{multipole}'")
+        if multipole != "mono" and form != "fp32":
+            raise ValueError(f"multipole must be 'mono', got '{multipole}' "
+                         "(form='fp32' also accepts 'quad')")
+        _lib.check(self.L.bhut_batch_set_multipole(self.h, _lib.MULTIPOLES[multipole]))
+        self.form, self.criterion, self.multipole = form, criterion, multipole
         self.targets_per_warp, self.use_graph = targets_per_warp, use_graph
 
     def load(self, positions, masses, offsets) -> "BatchedSolver":
@@ -121,11 +127,13 @@ class BatchedSolver:
 
 def batched_accelerations(systems, *, theta: float = 0.5, softening: float = 0.0,
                           G: float = 1.0, leaf_size: int = 32, form: str = "fp32",
-                          criterion: str = "bh", targets_per_warp: int = 32):
+                          criterion: str = "bh", targets_per_warp: int = 32,
+                          multipole: str = "mono"):
     """Self accelerations of every (positions, masses) system; returns a list."""
     pos, m, off = concat_systems(systems)
     dim = pos.shape[1]
     sv = BatchedSolver(dim=dim, leaf_size=leaf_size, form=form, criterion=criterion,
+                       multipole=multipole,
                        targets_per_warp=targets_per_warp, use_graph=False)
     try:
         sv.load(pos, m, off)
@@ -137,7 +145,7 @@ def batched_accelerations(systems, *, theta: float = 0.5, softening: float = 0.0
 
 def autotune(positions, masses, offsets, *, theta: float, softening: float, G: float = 1.0,
              form: str = "fp32", criterion: str = "bh", leaf_sizes=(8, 16, 32, 64),
-             targets_per_warp=(32, 16), repeats: int = 2):
+             targets_per_warp=(32, 16), repeats: int = 2, multipole: str = "mono"):
     """Times every (leaf_size, targets_per_warp) candidate on this batch
     (graph replay, warm) and returns (best config, {config: seconds})."""
     import torch
@@ -153,7 +161,7 @@ def autotune(positions, masses, offsets, *, theta: float, softening: float, G: f
             if tpw != 32 and dim != 3:
                 continue
             sv = BatchedSolver(dim=dim, leaf_size=L, form=form, criterion=criterion,
-                               targets_per_warp=tpw, use_graph=True)
+                               targets_per_warp=tpw, use_graph=True, multipole=multipole)
             sv.load(pos, m, offsets)
             out = torch.empty((int(offsets[-1]), dim), dtype=torch.float64, device="cuda")
             best = float("inf")

@@ -236,7 +236,8 @@ k_seg_frames(TreeDev t, const int64_t* __restrict__ part_off, const int64_t* __r
              const double* __restrict__ box, const double* __restrict__ center,
              FastFrame* __restrict__ frames, float4* __restrict__ ph, float4* __restrict__ pl,
              float4* __restrict__ nh, float4* __restrict__ nl, float* __restrict__ nsize,
-             float* __restrict__ ndelta)
+             float* __restrict__ ndelta, const double* __restrict__ quad, float4* __restrict__ nq0,
+             float2* __restrict__ nq1)
 {
     const int s = blockIdx.x;
     const int dim = t.dim;
@@ -274,6 +275,13 @@ k_seg_frames(TreeDev t, const int64_t* __restrict__ part_off, const int64_t* __r
             dd += v * v;
         }
         ndelta[k] = __double2float_ru(sqrt(dd) * f.s);
+        if (quad) {   // mass x length^2: scale by ms s^2
+            const double qs = f.ms * f.s * f.s;
+            const double* q = quad + 6 * k;
+            nq0[k] = make_float4((float)(q[0] * qs), (float)(q[1] * qs), (float)(q[2] * qs),
+                                 (float)(q[3] * qs));
+            nq1[k] = make_float2((float)(q[4] * qs), (float)(q[5] * qs));
+        }
     }
 }
 
@@ -291,6 +299,8 @@ struct BatchDev {
     const float4* nl;
     const float* nsize;
     const float* ndelta;
+    const float4* nq0;            // quadrupoles (FP32 form); NULL: monopoles
+    const float2* nq1;
 };
 
 struct BatchArgs {
@@ -431,7 +441,11 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                 const unsigned omask = __ballot_sync(FULL, act && open);
                 if (act && !open && sub == 0) {
                     if (FP32) {
-                        pair_f32<DIM>(Th, Tl, nhv, nlv, e2h, ah, al);
+                        if (b.nq0)
+                            node_quad_f32<DIM>(Th, Tl, nhv, nlv, b.nq0[node], b.nq1[node], e2h,
+                                               ah, al);
+                        else
+                            pair_f32<DIM>(Th, Tl, nhv, nlv, e2h, ah, al);
                     } else if (!pair_ff<DIM, false>(Th, Tl, nhv, nlv, e2h, e2l, ah, al)) {
                         const NodeCM cm = t.cm[node];
                         pair_fp64<DIM>(x, y, z, cm.x, cm.y, cm.z, cm.w, eps2, a64);
@@ -515,6 +529,7 @@ struct BufB {
 
 struct bhut_batch {
     int dim = 3, leaf = 32, form = BHUT_FORM_FP32, mac = 0, tpw = 32;
+    int multipole = BHUT_MULTIPOLE_MONO;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int64_t nsys = 0, ntot = 0, mtot = 0, ltot = 0;
@@ -524,7 +539,7 @@ struct bhut_batch {
     BufB pos, mass, d_part_off, d_node_off, d_leaf_off, d_tasks, keys, perm, sys_of, key2,
         sx, sy, sz, sm, cm, size, center, half, lo, hi, first_child, start, count, parent,
         leaf_list, arrive, sort_scratch, box, frames, ph, pl, nh, nl, nsize, ndelta, counter,
-        err, stats, out, keep, perm_in;
+        err, stats, out, keep, perm_in, quad, nq0, nq1;
     bool keep_active = false;
     unsigned long long last_stats[5] = {0, 0, 0, 0, 0};
     cudaGraphExec_t graph = nullptr;
@@ -536,7 +551,7 @@ struct bhut_batch {
                      &sys_of, &key2, &sx, &sy, &sz, &sm, &cm, &size, &center, &half, &lo, &hi,
                      &first_child, &start, &count, &parent, &leaf_list, &arrive, &sort_scratch,
                      &box, &frames, &ph, &pl, &nh, &nl, &nsize, &ndelta, &counter, &err, &stats,
-                     &out, &keep, &perm_in, nullptr};
+                     &out, &keep, &perm_in, &quad, &nq0, &nq1, nullptr};
 
     TreeDev dev() const
     {
@@ -639,6 +654,9 @@ int plan_layout(bhut_batch* b, const int64_t* offsets, int64_t nsys)
     BHUT_TRY(b->nl.ensure(sizeof(float4) * mtot, s));
     BHUT_TRY(b->nsize.ensure(sizeof(float) * mtot, s));
     BHUT_TRY(b->ndelta.ensure(sizeof(float) * mtot, s));
+    BHUT_TRY(b->quad.ensure(sizeof(double) * 6 * mtot, s));
+    BHUT_TRY(b->nq0.ensure(sizeof(float4) * mtot, s));
+    BHUT_TRY(b->nq1.ensure(sizeof(float2) * mtot, s));
     BHUT_TRY(b->box.ensure(sizeof(double) * 8 * nsys, s));
     BHUT_TRY(b->frames.ensure(sizeof(FastFrame) * nsys, s));
     BHUT_TRY(b->sort_scratch.ensure(sort_scratch_bytes(b->ntot), s));
@@ -707,10 +725,18 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
                               b->count.as<int32_t>(), b->parent.as<int32_t>(),
                               b->arrive.as<unsigned>(), o, false, nullptr, nullptr,
                               b->err.as<unsigned>(), s));
+    const bool quad = b->form == BHUT_FORM_FP32 && b->multipole == BHUT_MULTIPOLE_QUAD;
+    if (quad)
+        BHUT_TRY(launch_quadrupoles(b->dev(), b->leaf_list.as<int32_t>(), b->ltot,
+                                    b->first_child.as<int32_t>(), b->start.as<int32_t>(),
+                                    b->count.as<int32_t>(), b->parent.as<int32_t>(),
+                                    b->arrive.as<unsigned>(), b->quad.as<double>(),
+                                    b->err.as<unsigned>(), s));
     k_seg_frames<<<(unsigned)ns, kSegThreads, 0, s>>>(
         b->dev(), b->d_part_off.as<int64_t>(), b->d_node_off.as<int64_t>(), b->box.as<double>(),
         b->center.as<double>(), b->frames.as<FastFrame>(), b->ph.as<float4>(), b->pl.as<float4>(),
-        b->nh.as<float4>(), b->nl.as<float4>(), b->nsize.as<float>(), b->ndelta.as<float>());
+        b->nh.as<float4>(), b->nl.as<float4>(), b->nsize.as<float>(), b->ndelta.as<float>(),
+        quad ? b->quad.as<double>() : nullptr, b->nq0.as<float4>(), b->nq1.as<float2>());
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
     // traversal
@@ -719,7 +745,8 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
     BatchDev bd{b->dev(), b->d_part_off.as<int64_t>(), b->d_node_off.as<int64_t>(),
                 b->frames.as<FastFrame>(), b->ph.as<float4>(), b->pl.as<float4>(),
                 b->nh.as<float4>(), b->nl.as<float4>(), b->nsize.as<float>(),
-                b->ndelta.as<float>()};
+                b->ndelta.as<float>(), quad ? b->nq0.as<float4>() : nullptr,
+                quad ? b->nq1.as<float2>() : nullptr};
     BatchArgs a{b->d_tasks.as<int2>(), (int)b->tasks.size(), b->counter.as<unsigned>(), theta,
                 eps, G, b->mac, out, b->err.as<unsigned>(), b->stats.as<unsigned long long>()};
     const unsigned grid = 152u * 6u;   // persistent: about one wave of resident blocks
@@ -820,6 +847,18 @@ int bhut_batch_configure(bhut_batch* b, int form, int criterion, int targets_per
     b->use_graph = use_graph != 0;
     drop_graph(b);
     if (retask && b->layout_valid) BHUT_TRY(plan_tasks(b));
+    return kOk;
+}
+
+int bhut_batch_set_multipole(bhut_batch* b, int multipole)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (multipole != BHUT_MULTIPOLE_MONO && multipole != BHUT_MULTIPOLE_QUAD) {
+        set_error("unknown multipole order %d", multipole);
+        return kInvalid;
+    }
+    if (multipole != b->multipole) drop_graph(b);
+    b->multipole = multipole;
     return kOk;
 }
 

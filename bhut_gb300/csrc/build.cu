@@ -436,6 +436,79 @@ __global__ void k_bottom_up(TreeDev t, const int32_t* __restrict__ leaf_list, in
     }
 }
 
+// Traceless quadrupole of every node about its centre of mass,
+// Q_ij = sum_k m_k (3 d_i d_j - |d|^2 delta_ij), d = x_k - com (used by the
+// FP32 forms with multipole "quad").  Leaves sum their particles; a parent
+// adds its children's moments shifted to its own centre of mass (parallel
+// axis: Q_c + M_c (3 d d^T - |d|^2 I), d = com_c - com_p).  Stored as
+// (xx, yy, zz, xy, xz, yz).  Same arrival-counter climb as k_bottom_up.
+__device__ __forceinline__ void quad_add(double* q, double m, double dx, double dy, double dz)
+{
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    q[0] += m * (3.0 * dx * dx - d2);
+    q[1] += m * (3.0 * dy * dy - d2);
+    q[2] += m * (3.0 * dz * dz - d2);
+    q[3] += m * (3.0 * dx * dy);
+    q[4] += m * (3.0 * dx * dz);
+    q[5] += m * (3.0 * dy * dz);
+}
+
+__global__ void k_quadrupoles(TreeDev t, const int32_t* __restrict__ leaf_list, int64_t num_leaves,
+                              const int32_t* __restrict__ first_child,
+                              const int32_t* __restrict__ start, const int32_t* __restrict__ count,
+                              const int32_t* __restrict__ parent, unsigned* __restrict__ arrive,
+                              double* __restrict__ quad, unsigned* __restrict__ err)
+{
+    for (int64_t li = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; li < num_leaves;
+         li += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t id = leaf_list[li];
+        if (id < 0 || id >= t.m) { atomicOr(err, kErrBadNode); continue; }
+        const NodeCM c = t.cm[id];
+        double q[6] = {0, 0, 0, 0, 0, 0};
+        const int64_t s = start[id], n = count[id];
+        for (int64_t i = s; i < s + n; i++)
+            quad_add(q, t.sm[i], t.sx[i] - c.x, t.sy[i] - c.y, t.dim == 3 ? t.sz[i] - c.z : 0.0);
+        for (int k = 0; k < 6; k++) quad[6 * (int64_t)id + k] = q[k];
+        int32_t node = id;
+        while (true) {
+            const int32_t p = parent[node];
+            if (p < 0) break;
+            if (p >= t.m || first_child[p] < 1 || first_child[p] + 1 >= t.m) {
+                atomicOr(err, kErrBadNode);
+                break;
+            }
+            __threadfence();
+            if (atomicAdd(&arrive[p], 1u) == 0) break;
+            __threadfence();
+            const NodeCM cp = t.cm[p];
+            double qp[6] = {0, 0, 0, 0, 0, 0};
+            for (int j = 0; j < 2; j++) {
+                const int32_t ch = first_child[p] + j;
+                const double2 a = __ldcg(reinterpret_cast<const double2*>(&t.cm[ch]));
+                const double2 b = __ldcg(reinterpret_cast<const double2*>(&t.cm[ch]) + 1);
+                for (int k = 0; k < 6; k++) qp[k] += __ldcg(&quad[6 * (int64_t)ch + k]);
+                quad_add(qp, b.y, a.x - cp.x, a.y - cp.y, t.dim == 3 ? b.x - cp.z : 0.0);
+            }
+            for (int k = 0; k < 6; k++) quad[6 * (int64_t)p + k] = qp[k];
+            node = p;
+        }
+    }
+}
+
+int launch_quadrupoles(const TreeDev& t, const int32_t* leaf_list, int64_t num_leaves,
+                       const int32_t* first_child, const int32_t* start, const int32_t* count,
+                       const int32_t* parent, unsigned* arrive, double* quad, unsigned* err,
+                       cudaStream_t s)
+{
+    BHUT_CUDA(cudaMemsetAsync(arrive, 0, sizeof(unsigned) * (size_t)t.m, s));
+    k_quadrupoles<<<grid_for(num_leaves, 128), 128, 0, s>>>(t, leaf_list, num_leaves, first_child,
+                                                            start, count, parent, arrive, quad,
+                                                            err);
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
+    return kOk;
+}
+
 // Refit-vs-rebuild test of refit.py:236-249: any particle with
 // max_axis |x - root_center| > 1.1 * root_half_size forces a rebuild.
 __global__ void k_outside_root(const double* __restrict__ pos, int64_t n, int dim,

@@ -112,9 +112,11 @@ struct bhut_tree {
     // traversal targets
     DevBuf tpos, tkeys, tperm, tx, ty, tz, tbox, out;
     // float-float copies for the fast form
-    DevBuf frame, ph, pl, nh, nl, nsize, ndelta, th, tl;
+    DevBuf frame, ph, pl, nh, nl, nsize, ndelta, th, tl, quad, nq0, nq1;
     bool ff_valid = false;
+    bool ff_quad = false;
     int mac = 0;
+    int multipole = BHUT_MULTIPOLE_MONO;
 
     TreeDev dev() const
     {
@@ -278,7 +280,8 @@ int finish_out(bhut_tree* t, const OutTarget& o, size_t bytes, const char* what)
 // per build/refit, on first use).
 int prepare_fast(bhut_tree* t)
 {
-    if (t->ff_valid) return kOk;
+    const bool want_quad = t->multipole == BHUT_MULTIPOLE_QUAD && t->form == BHUT_FORM_FP32;
+    if (t->ff_valid && t->ff_quad == want_quad) return kOk;
     cudaStream_t s = t->stream;
     BHUT_TRY(t->frame.ensure(sizeof(FastFrame), s));
     BHUT_TRY(t->ph.ensure(sizeof(float4) * t->n, s));
@@ -287,10 +290,23 @@ int prepare_fast(bhut_tree* t)
     BHUT_TRY(t->nl.ensure(sizeof(float4) * t->m, s));
     BHUT_TRY(t->nsize.ensure(sizeof(float) * t->m, s));
     BHUT_TRY(t->ndelta.ensure(sizeof(float) * t->m, s));
+    const bool quad = t->multipole == BHUT_MULTIPOLE_QUAD && t->form == BHUT_FORM_FP32;
+    if (quad) {
+        BHUT_TRY(t->quad.ensure(sizeof(double) * 6 * t->m, s));
+        BHUT_TRY(t->nq0.ensure(sizeof(float4) * t->m, s));
+        BHUT_TRY(t->nq1.ensure(sizeof(float2) * t->m, s));
+        BHUT_TRY(launch_quadrupoles(t->dev(), t->leaf_list.as<int32_t>(), t->tt.num_leaves,
+                                    t->first_child.as<int32_t>(), t->start.as<int32_t>(),
+                                    t->count.as<int32_t>(), t->parent.as<int32_t>(),
+                                    t->arrive.as<unsigned>(), t->quad.as<double>(),
+                                    t->err.as<unsigned>(), s));
+    }
     BHUT_TRY(launch_fast_prepare(t->box.as<double>(), t->dim, t->frame.as<FastFrame>(), t->dev(),
                                  t->center.as<double>(), t->ph.as<float4>(), t->pl.as<float4>(),
                                  t->nh.as<float4>(), t->nl.as<float4>(), t->nsize.as<float>(),
-                                 t->ndelta.as<float>(), s));
+                                 t->ndelta.as<float>(), quad ? t->quad.as<double>() : nullptr,
+                                 t->nq0.as<float4>(), t->nq1.as<float2>(), s));
+    t->ff_quad = quad;
     t->ff_valid = true;
     return kOk;
 }
@@ -299,7 +315,8 @@ FastTree fast_tree(const bhut_tree* t)
 {
     return FastTree{t->frame.as<FastFrame>(), t->ph.as<float4>(), t->pl.as<float4>(),
                     t->nh.as<float4>(), t->nl.as<float4>(), t->nsize.as<float>(),
-                    t->ndelta.as<float>()};
+                    t->ndelta.as<float>(), t->ff_quad ? t->nq0.as<float4>() : nullptr,
+                    t->ff_quad ? t->nq1.as<float2>() : nullptr};
 }
 
 // Scale of the fast form's normalised coordinates (the frame's s), read
@@ -466,6 +483,17 @@ int bhut_tree_set_form(bhut_tree* t, int form)
     return kOk;
 }
 
+int bhut_tree_set_multipole(bhut_tree* t, int multipole)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (multipole != BHUT_MULTIPOLE_MONO && multipole != BHUT_MULTIPOLE_QUAD) {
+        set_error("unknown multipole order %d", multipole);
+        return kInvalid;
+    }
+    t->multipole = multipole;
+    return kOk;
+}
+
 int bhut_tree_set_criterion(bhut_tree* t, int criterion)
 {
     if (!t) { set_error("tree is NULL"); return kInvalid; }
@@ -606,7 +634,7 @@ void bhut_tree_destroy(bhut_tree* t)
                      &t->sort_scratch, &t->box_partial, &t->box, &t->counters, &t->err, &t->stats,
                      &t->tpos, &t->tkeys, &t->tperm, &t->tx, &t->ty, &t->tz, &t->tbox, &t->out,
                      &t->frame, &t->ph, &t->pl, &t->nh, &t->nl, &t->nsize, &t->ndelta, &t->th,
-                     &t->tl};
+                     &t->tl, &t->quad, &t->nq0, &t->nq1};
     for (DevBuf* b : all) b->release(s);
     cudaStreamSynchronize(s);
     if (t->own_stream) cudaStreamDestroy(s);

@@ -211,4 +211,39 @@ __device__ __forceinline__ void pair_f32(const float* Th, const float* Tl, float
 }
 
 
+// A node's monopole plus its Plummer-softened traceless quadrupole (FP32
+// form, multipole "quad"), Kahan-added.  With d = com - x (target to node),
+// r^2 = |d|^2 + eps^2:
+//   a = M d / r^3 - Q d / r^5 + (5/2) (d . Q d) d / r^7,
+// the gradient of the potential -M/r - (1/2) d.Q d / r^5.
+template <int DIM>
+__device__ __forceinline__ void node_quad_f32(const float* Th, const float* Tl, float4 nh,
+                                              float4 nl, float4 q0, float2 q1, float e2,
+                                              float* acc, float* cmp)
+{
+    const float d0 = __fadd_rn(__fsub_rn(nh.x, Th[0]), __fsub_rn(nl.x, Tl[0]));
+    const float d1 = __fadd_rn(__fsub_rn(nh.y, Th[1]), __fsub_rn(nl.y, Tl[1]));
+    const float d2 = DIM == 3 ? __fadd_rn(__fsub_rn(nh.z, Th[2]), __fsub_rn(nl.z, Tl[2])) : 0.0f;
+    float r2 = fmaf(d1, d1, fmaf(d0, d0, e2));
+    if (DIM == 3) r2 = fmaf(d2, d2, r2);
+    if (!(r2 > 0.0f)) return;
+    const float ri = rsqrtf(r2);
+    const float ri2 = ri * ri;
+    const float ri3 = ri2 * ri;
+    const float ri5 = ri3 * ri2;
+    const float qx = fmaf(q1.x, d2, fmaf(q0.w, d1, q0.x * d0));
+    const float qy = fmaf(q1.y, d2, fmaf(q0.y, d1, q0.w * d0));
+    const float qz = fmaf(q0.z, d2, fmaf(q1.y, d1, q1.x * d0));
+    const float dqd = fmaf(d2, qz, fmaf(d1, qy, d0 * qx));
+    const float f = fmaf(2.5f * dqd, ri5 * ri2, nh.w * ri3);
+    const float d[3] = {d0, d1, d2}, q[3] = {qx, qy, qz};
+#pragma unroll
+    for (int k = 0; k < DIM; k++) {
+        const float y = __fsub_rn(fmaf(f, d[k], -ri5 * q[k]), cmp[k]);
+        const float t = __fadd_rn(acc[k], y);
+        cmp[k] = __fsub_rn(__fsub_rn(t, acc[k]), y);
+        acc[k] = t;
+    }
+}
+
 }  // namespace bhut

@@ -68,7 +68,8 @@ __global__ void k_ff_nodes(const NodeCM* __restrict__ cm, const double* __restri
                            const double* __restrict__ center, int64_t m, int dim,
                            const FastFrame* __restrict__ fr, float4* __restrict__ nh,
                            float4* __restrict__ nl, float* __restrict__ nsize,
-                           float* __restrict__ ndelta)
+                           float* __restrict__ ndelta, const double* __restrict__ quad,
+                           float4* __restrict__ nq0, float2* __restrict__ nq1)
 {
     const FastFrame f = *fr;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m;
@@ -92,6 +93,13 @@ __global__ void k_ff_nodes(const NodeCM* __restrict__ cm, const double* __restri
             dd += v * v;
         }
         ndelta[k] = __double2float_ru(sqrt(dd) * f.s);
+        if (quad) {   // mass x length^2: scale by ms s^2
+            const double qs = f.ms * f.s * f.s;
+            const double* q = quad + 6 * k;
+            nq0[k] = make_float4((float)(q[0] * qs), (float)(q[1] * qs), (float)(q[2] * qs),
+                                 (float)(q[3] * qs));
+            nq1[k] = make_float2((float)(q[4] * qs), (float)(q[5] * qs));
+        }
     }
 }
 
@@ -384,7 +392,11 @@ __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, c
             }
             const unsigned omask = __ballot_sync(FULL, act && open);
             if (act && !open) {
-                pair_f32<DIM>(T, Tl, nh, ft.nl[node], a.e2h, acc, cmp);
+                if (ft.nq0)
+                    node_quad_f32<DIM>(T, Tl, nh, ft.nl[node], ft.nq0[node], ft.nq1[node], a.e2h,
+                                       acc, cmp);
+                else
+                    pair_f32<DIM>(T, Tl, nh, ft.nl[node], a.e2h, acc, cmp);
                 cnt[1]++;
             }
             if (omask) {
@@ -449,13 +461,14 @@ k_traverse_fp32(TreeDev t, FastTree ft, FastArgs a)
 // ---------------------------------------------------------------------------
 int launch_fast_prepare(const double* box, int dim, FastFrame* frame, const TreeDev& t,
                         const double* center, float4* ph, float4* pl, float4* nh, float4* nl,
-                        float* nsize, float* ndelta, cudaStream_t s)
+                        float* nsize, float* ndelta, const double* quad, float4* nq0,
+                        float2* nq1, cudaStream_t s)
 {
     k_frame<<<1, 32, 0, s>>>(box, dim, frame);
     k_ff_particles<<<grid_for(t.n, 256), 256, 0, s>>>(t.sx, t.sy, t.sz, t.sm, t.n, dim, frame, ph,
                                                       pl);
     k_ff_nodes<<<grid_for(t.m, 256), 256, 0, s>>>(t.cm, t.size, center, t.m, dim, frame, nh, nl,
-                                                  nsize, ndelta);
+                                                  nsize, ndelta, quad, nq0, nq1);
     BHUT_CUDA(cudaGetLastError());
     note_launches(3);
     return kOk;

@@ -67,6 +67,8 @@ struct FastTree {
     const float4* nl;   // (com, mass) lo per node
     const float* nsize; // 2 * half_size, normalised, per node
     const float* ndelta; // |com - AABB centre|, normalised, per node (offset criterion)
+    const float4* nq0;   // quadrupole (xx, yy, zz, xy), normalised, per node; NULL: monopoles
+    const float2* nq1;   // quadrupole (xz, yz)
 };
 
 // Morton encoding (bhut/utils/morton.py:14-45, 183-198) and the quantisation
@@ -141,6 +143,10 @@ int launch_bottom_up(const TreeDev& t, const int32_t* leaf_list, int64_t num_lea
                      const int32_t* first_child, const int32_t* start, const int32_t* count,
                      const int32_t* parent, unsigned* arrive, NodeOut o, bool refit,
                      const double* opos, const double* omass, unsigned* err, cudaStream_t s);
+int launch_quadrupoles(const TreeDev& t, const int32_t* leaf_list, int64_t num_leaves,
+                       const int32_t* first_child, const int32_t* start, const int32_t* count,
+                       const int32_t* parent, unsigned* arrive, double* quad, unsigned* err,
+                       cudaStream_t s);
 int launch_outside_root(const double* pos, int64_t n, int dim, const double* center0,
                         const double* half0, unsigned* flag, cudaStream_t s);
 int launch_traverse_exact(const TreeDev& t, const double* tx, const double* ty, const double* tz,
@@ -149,7 +155,8 @@ int launch_traverse_exact(const TreeDev& t, const double* tx, const double* ty, 
                           unsigned long long* stats, cudaStream_t s);
 int launch_fast_prepare(const double* box, int dim, FastFrame* frame, const TreeDev& t,
                         const double* center, float4* ph, float4* pl, float4* nh, float4* nl,
-                        float* nsize, float* ndelta, cudaStream_t s);
+                        float* nsize, float* ndelta, const double* quad, float4* nq0,
+                        float2* nq1, cudaStream_t s);
 int launch_fast_targets(const double* tx, const double* ty, const double* tz, int64_t nt, int dim,
                         const FastFrame* frame, float4* th, float4* tl, cudaStream_t s);
 int launch_traverse_fast(const TreeDev& t, const FastTree& ft, const float4* th, const float4* tl,

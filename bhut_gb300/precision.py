@@ -54,7 +54,7 @@ def sampled_errors(positions, masses, acc, *, softening: float, G: float = 1.0,
 
 
 def autotune_leaf_size(positions, masses, *, theta: float, softening: float, G: float = 1.0,
-                       form: str = "fp32", criterion: str = "bh",
+                       form: str = "fp32", criterion: str = "bh", multipole: str = "mono",
                        candidates=(8, 16, 32, 64), repeats: int = 2) -> tuple[int, dict]:
     """Builds a tree per candidate leaf size and times build + self traversal;
     returns (best leaf size, {leaf_size: seconds})."""
@@ -68,7 +68,8 @@ def autotune_leaf_size(positions, masses, *, theta: float, softening: float, G: 
     m = dev(masses)
     times = {}
     for L in candidates:
-        tree = api.Tree(pos, m, leaf_size=L, form=form, criterion=criterion)
+        tree = api.Tree(pos, m, leaf_size=L, form=form, criterion=criterion,
+                        multipole=multipole)
         best = float("inf")
         for r in range(repeats + 1):
             torch.cuda.synchronize()

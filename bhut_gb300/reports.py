@@ -42,7 +42,8 @@ def _log(msg):
 
 
 def precision_report(n: int = 4_000_000, n_sample: int = 8192, thetas=(0.3, 0.5, 0.7),
-                     eps: float = 0.005, G: float = 1.0, seed: int = 7, criterion: str = "bh"):
+                     eps: float = 0.005, G: float = 1.0, seed: int = 7, criterion: str = "bh",
+                     multipole: str = "mono"):
     import torch
     pos, m = workloads.galaxy(n, seed=seed)
     _log(f"galaxy N={n} generated")
@@ -56,9 +57,11 @@ def precision_report(n: int = 4_000_000, n_sample: int = 8192, thetas=(0.3, 0.5,
     lines = []
     for theta in thetas:
         leaf, times = precision.autotune_leaf_size(pd, md, theta=theta, softening=eps, G=G,
-                                                   form="fp32", criterion=criterion)
+                                                   form="fp32", criterion=criterion,
+                                                   multipole=multipole)
         _log(f"theta={theta}: autotune {times}")
-        t32 = api.Tree(pd, md, leaf_size=leaf, form="fp32", criterion=criterion).build()
+        t32 = api.Tree(pd, md, leaf_size=leaf, form="fp32", criterion=criterion,
+                       multipole=multipole).build()
         a32, s32 = _timed_solve(t32, theta, eps, G)
         p2p, m2p, _ = t32._handle.stats()
         t32.close()
@@ -73,7 +76,7 @@ def precision_report(n: int = 4_000_000, n_sample: int = 8192, thetas=(0.3, 0.5,
         line = {
             "report": "precision", "workload": f"galaxy N={n:,} (70% exponential disc Rd=3, "
             "z0=0.3; 30% Hernquist bulge a=0.5; equal masses)", "theta": theta,
-            "softening": eps, "criterion": criterion, "leaf_size": leaf,
+            "softening": eps, "criterion": criterion, "multipole": multipole, "leaf_size": leaf,
             "autotune_s": {str(k): v for k, v in times.items()},
             "fp32": {"accels_per_s": n / s32, "solve_ms": 1e3 * s32,
                      "err_vs_direct": precision.error_distribution(a32h[idx], ref),
@@ -91,7 +94,8 @@ def precision_report(n: int = 4_000_000, n_sample: int = 8192, thetas=(0.3, 0.5,
 
 def batched_report(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: int = 11,
                    theta: float = 0.5, eps: float = 0.01, G: float = 1.0, reps: int = 3,
-                   plain_sample: int = 64, err_systems: int = 16, criterion: str = "bh"):
+                   plain_sample: int = 64, err_systems: int = 16, criterion: str = "bh",
+                   multipole: str = "mono"):
     """``batched``: nsys Plummer spheres (N log-uniform in [nmin, nmax], scale
     radius uniform in [0.5, 2], own seeds, equal masses 1/N) solved in one
     batch (FP32 form, CUDA graph, autotuned leaf size and targets per warp);
@@ -107,10 +111,11 @@ def batched_report(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: i
     pd = torch.as_tensor(pos).cuda()
     md = torch.as_tensor(m).cuda()
     cfg, times = batch.autotune(pd, md, off, theta=theta, softening=eps, G=G, form="fp32",
-                                criterion=criterion)
+                                criterion=criterion, multipole=multipole)
     _log(f"autotune {cfg} {times}")
     sv = batch.BatchedSolver(leaf_size=cfg["leaf_size"], form="fp32", criterion=criterion,
-                             targets_per_warp=cfg["targets_per_warp"], use_graph=True)
+                             targets_per_warp=cfg["targets_per_warp"], use_graph=True,
+                             multipole=multipole)
     sv.load(pd, md, off)
     out = torch.empty_like(pd)
     sv.solve(theta=theta, softening=eps, G=G, out=out)
@@ -154,7 +159,8 @@ def batched_report(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: i
     line = {
         "report": "batched", "workload": f"{nsys} Plummer spheres, N log-uniform in "
         f"[{nmin}, {nmax}], a ~ U[0.5, 2], own seeds", "particles": ntot, "theta": theta,
-        "softening": eps, "form": "fp32", "criterion": criterion, "config": cfg,
+        "softening": eps, "form": "fp32", "criterion": criterion, "multipole": multipole,
+        "config": cfg,
         "autotune_s": {f"L{k[0]}_tpw{k[1]}": v for k, v in times.items()},
         "solve_ms": t_batch * 1e3, "systems_per_s": nsys / t_batch,
         "accels_per_s": ntot / t_batch, "interactions": {"p2p": p2p, "m2p": m2p},
@@ -169,7 +175,8 @@ def batched_report(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: i
 
 
 def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: int = 21,
-                  plain_seconds: float = 90.0, err_requests: int = 4):
+                  plain_seconds: float = 90.0, err_requests: int = 4,
+                  criterion: str = "bh_offset", multipole: str = "mono"):
     """``served``: a Poisson stream (mean ``rate`` requests/s) of ``count``
     systems (N log-uniform in [1e3, 2e6], half Plummer, half uniform cubes of
     side 2, velocities N(0, 0.1^2)), each advanced ``steps`` KDK steps
@@ -189,13 +196,14 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
         idx = precision.sample_indices(r.n, 2048, seed=1)
         ref = precision.direct_reference(r.positions, r.masses, idx, softening=0.01)
         a_s = api.accelerations(r.positions, r.masses, theta=0.5, softening=0.01,
-                                form="fp32", criterion="bh_offset")
+                                form="fp32", criterion=criterion, multipole=multipole,
+                                leaf_size=16)
         a_p = api.accelerations(r.positions, r.masses, theta=0.5, softening=0.01, form="fast")
         errs_srv.append(precision.error_distribution(a_s[idx], ref)["median"])
         errs_plain.append(precision.error_distribution(a_p[idx], ref)["median"])
     _log(f"median errors: served {errs_srv}, plain {errs_plain}")
     sv = serve.Server(theta=0.5, softening=0.01, dt=1e-3, rebuild_every=10, form="fp32",
-                      criterion="bh_offset")
+                      criterion=criterion, multipole=multipole)
     st = sv.run(reqs, realtime=True)
     sv.close()
     _log(f"served: {st}")
@@ -204,10 +212,11 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
                           realtime=True, max_seconds=plain_seconds)
     _log(f"plain: {pl}")
     line = {"report": "served", "requests": count, "rate_per_s": rate, "steps": steps,
-            "particles": total_n, "served": st, "plain": pl,
+            "particles": total_n, "criterion": criterion, "multipole": multipole,
+            "served": st, "plain": pl,
             "solves_per_s_ratio": st["solves_per_s"] / pl["solves_per_s"]
             if pl["solves_per_s"] else None,
-            "median_err_vs_direct": {"served_fp32_offset": float(np.median(errs_srv)),
+            "median_err_vs_direct": {"served_fp32": float(np.median(errs_srv)),
                                      "plain_fast_bh": float(np.median(errs_plain))}}
     print(json.dumps(line), flush=True)
     return line
@@ -220,16 +229,19 @@ def main():
     ap.add_argument("--nsys", type=int, default=2048)
     ap.add_argument("--n", type=int, default=4_000_000)
     ap.add_argument("--sample", type=int, default=8192)
-    ap.add_argument("--criterion", default="bh")
+    ap.add_argument("--criterion", default=None)
+    ap.add_argument("--multipole", default="mono")
     ap.add_argument("--thetas", default="0.3,0.5,0.7")
     args = ap.parse_args()
     if args.report == "precision":
-        precision_report(args.n, args.sample, criterion=args.criterion,
+        precision_report(args.n, args.sample, criterion=args.criterion or "bh",
+                         multipole=args.multipole,
                          thetas=tuple(float(x) for x in args.thetas.split(",")))
     elif args.report == "batched":
-        batched_report(args.nsys, criterion=args.criterion)
+        batched_report(args.nsys, criterion=args.criterion or "bh", multipole=args.multipole)
     elif args.report == "served":
-        served_report(args.count)
+        served_report(args.count, criterion=args.criterion or "bh_offset",
+                      multipole=args.multipole)
 
 
 if __name__ == "__main__":

@@ -34,10 +34,10 @@ from .batch import BatchedSolver
 
 # Device bytes per resident particle: request state (x, v, a, m, order),
 # the batch's copies, sort scratch and float-float particles, and the node
-# arrays (about 2 N / leaf_size nodes of ~190 B).
+# arrays (about 2 N / leaf_size nodes of ~190 B, plus 72 B of quadrupoles).
 STATE_BYTES = 3 * 24 + 8 + 4
 BATCH_BYTES = 24 + 8 + 8 + 8 + 4 + 4 + 32 + 32 + 12 + 4 + 24
-NODE_BYTES = 190
+NODE_BYTES = 262
 
 
 def bytes_per_particle(leaf_size: int) -> float:
@@ -105,7 +105,8 @@ class Server:
     def __init__(self, *, theta: float = 0.5, softening: float = 0.01, G: float = 1.0,
                  dt: float = 1e-3, rebuild_every: int = 10, form: str = "fp32",
                  criterion: str = "bh_offset", leaf_size: int = 16, targets_per_warp: int = 32,
-                 hbm_budget: float = 150e9, max_active_particles: int | None = None):
+                 hbm_budget: float = 150e9, max_active_particles: int | None = None,
+                 multipole: str = "mono"):
         import torch
         self.torch = torch
         self.theta, self.eps, self.G, self.dt = theta, softening, G, dt
@@ -117,7 +118,7 @@ class Server:
         self.stream = torch.cuda.current_stream().cuda_stream
         self.solver = BatchedSolver(dim=3, leaf_size=leaf_size, form=form, criterion=criterion,
                                     targets_per_warp=targets_per_warp, use_graph=False,
-                                    stream=self.stream)
+                                    stream=self.stream, multipole=multipole)
         self.active: list[Request] = []
         self.finished: list[Request] = []
         self.ticks = 0

@@ -48,6 +48,10 @@ extern "C" {
 #define BHUT_MAC_BH 0      /* 2 h / |x - com| >= theta -> open (bhut/traverse/bh.py:576-601) */
 #define BHUT_MAC_OFFSET 1  /* open when |x - com| < 2 h / theta + |com - AABB centre| */
 
+/* Node expansions (bhut_tree_set_multipole, bhut_batch_set_multipole). */
+#define BHUT_MULTIPOLE_MONO 0  /* monopole (bhut/traverse/kernels.py:136-168) */
+#define BHUT_MULTIPOLE_QUAD 1  /* monopole + traceless quadrupole, FP32 form only */
+
 typedef struct bhut_tree bhut_tree;
 
 /* Library version string. */
@@ -112,6 +116,11 @@ BHUT_API long long bhut_launch_count(void);
  * in the reference, whose only criterion is "bh" (bhut/api.py:306-307). */
 BHUT_API int bhut_tree_set_criterion(bhut_tree *t, int criterion);
 
+/* Node expansion of the FP32 form (BHUT_MULTIPOLE_*; default monopole).  The
+ * exact and fast forms always use monopoles.  No counterpart in the
+ * reference, whose only multipole is "mono" (bhut/api.py:308-309). */
+BHUT_API int bhut_tree_set_multipole(bhut_tree *t, int multipole);
+
 /* n, node count, dim, leaf size of a built tree. */
 BHUT_API int bhut_tree_info(const bhut_tree *t, int64_t *n, int64_t *num_nodes, int *dim, int *leaf_size);
 
@@ -161,6 +170,10 @@ BHUT_API int bhut_batch_create(int dim, int leaf_size, void *stream, bhut_batch 
  * layout, theta, softening, G and output buffer stay the same. */
 BHUT_API int bhut_batch_configure(bhut_batch *b, int form, int criterion, int targets_per_warp,
                                   int use_graph);
+
+/* Node expansion of the batched FP32 form (BHUT_MULTIPOLE_*; default
+ * monopole); no counterpart in the reference. */
+BHUT_API int bhut_batch_set_multipole(bhut_batch *b, int multipole);
 
 /* Copies the systems in; a new layout (offsets) re-plans node counts, buffers
  * and the task queue. */

@@ -20,23 +20,25 @@ def systems():
     return workloads.plummer_batch(nsys=40, nmin=64, nmax=6000, seed=3)
 
 
-def _single(pos, m, form, theta=0.5, eps=0.01, leaf=32):
-    t = bh.Tree(pos, m, leaf_size=leaf, form=form).build()
+def _single(pos, m, form, theta=0.5, eps=0.01, leaf=32, multipole="mono"):
+    t = bh.Tree(pos, m, leaf_size=leaf, form=form, multipole=multipole).build()
     a = t.accelerations(theta=theta, softening=eps)
     st = t._handle.stats()
     t.close()
     return a, st
 
 
-@pytest.mark.parametrize("form", ["fast", "fp32"])
-def test_batch_equals_single_tree(systems, form):
+@pytest.mark.parametrize("form,multipole", [("fast", "mono"), ("fp32", "mono"),
+                                            ("fp32", "quad")])
+def test_batch_equals_single_tree(systems, form, multipole):
     pos, m, off = batch.concat_systems(systems)
-    sv = batch.BatchedSolver(form=form, targets_per_warp=32, use_graph=False)
+    sv = batch.BatchedSolver(form=form, targets_per_warp=32, use_graph=False,
+                             multipole=multipole)
     sv.load(pos, m, off)
     acc = sv.solve(theta=0.5, softening=0.01)
     p2p_tot = 0
     for s, (p, mm) in enumerate(systems):
-        ref, st = _single(p, mm, form)
+        ref, st = _single(p, mm, form, multipole=multipole)
         assert np.array_equal(acc[off[s]:off[s + 1]], ref), s
         p2p_tot += st[0]
     assert sv.stats()[0] == p2p_tot
