@@ -11,7 +11,9 @@ from .api import (  # noqa: F401
     Tree,
     TreeData,
     accelerations,
+    accelerations_chunks,
     build_tree,
+    compute_tree_statistics,
     direct_accelerations,
     morton_argsort,
     morton_keys,

@@ -59,6 +59,8 @@ SIGNATURES = {
     "bhut_morton_keys": (_INT, [_VP, _I64, _INT, _VP, _VP]),
     "bhut_morton_argsort": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),
     "bhut_direct_accelerations": (_INT, [_VP, _VP, _I64, _INT, _VP, _I64, _D, _D, _VP, _VP]),
+    "bhut_tree_statistics": (_INT, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _I64, _INT, _VP, _I64, _D,
+                                    _VP, _VP]),
     "bhut_morton_argsort_noalloc": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),
     "bhut_batch_create": (_INT, [_INT, _INT, _VP, ctypes.POINTER(_VP)]),
     "bhut_batch_configure": (_INT, [_VP, _INT, _INT, _INT, _INT]),

@@ -360,6 +360,31 @@ def accelerations(
     return out
 
 
+def accelerations_chunks(position_chunks, mass_chunks, *, theta: float = 0.5,
+                         softening: float = 0.0, G: float = 1.0, dim: int = 3,
+                         leaf_size: int = 32, form: str | None = None) -> list:
+    """The chunked self-acceleration path of bhut/api.py:28-78 without Dask:
+    the tree is built once over all chunks, each chunk's particles are then
+    evaluated as targets (no self skip, as the reference's map_blocks call of
+    barnes_hut_accelerations_targets; a particle's own zero-distance pair
+    contributes nothing) and the results come back in the same chunks."""
+    pos = [_to_f64(c) for c in position_chunks]
+    ms = [_to_f64(c) for c in mass_chunks]
+    if len(pos) != len(ms):
+        raise ValueError("position and mass chunk counts differ")
+    if pos and _is_cuda_tensor(pos[0]):
+        torch = _torch()
+        p_all, m_all = torch.cat(pos), torch.cat([m.to(pos[0].device) for m in ms])
+    else:
+        p_all = np.concatenate([np.asarray(_host(c)) for c in pos])
+        m_all = np.concatenate([np.asarray(_host(c)) for c in ms])
+    tree = Tree(p_all, m_all, leaf_size=leaf_size, dim=dim, form=form).build()
+    try:
+        return tree.accelerations_chunks(pos, theta=theta, softening=softening, G=G)
+    finally:
+        tree.close()
+
+
 def build_tree(positions, masses, *, leaf_size: int, backend: str, dim: int) -> TreeData:
     """bhut/api.py:155-191: build and return the TreeData arrays."""
     _check_backend(positions, backend)
@@ -514,6 +539,29 @@ class Tree:
             self._handle.accel_targets(targets, theta, eps, G, out)
         return out
 
+    def accelerations_chunks(self, target_chunks, *, theta: float = 0.5, softening: float = 0.0,
+                             G: float = 1.0) -> list:
+        """Chunks in, chunks out: the map_blocks path of bhut/api.py:690-731
+        without Dask.  The chunks are evaluated in ONE traversal launch over
+        their concatenation (each target's result does not depend on which
+        other targets share the launch) and the result is returned split
+        into chunks of the same lengths, as CUDA tensors for CUDA chunks."""
+        chunks = [_to_f64(c) for c in target_chunks]
+        if not chunks:
+            return []
+        for c in chunks:
+            if len(_shape(c)) != 2 or _shape(c)[1] != self.dim:
+                raise ValueError(f"target chunk has shape {_shape(c)}, expected (k, {self.dim})")
+        sizes = [_shape(c)[0] for c in chunks]
+        if _is_cuda_tensor(chunks[0]):
+            torch = _torch()
+            allt = torch.cat([c.to(chunks[0].device) for c in chunks])
+            out = self.accelerations(allt, theta=theta, softening=softening, G=G)
+            return list(torch.split(out, sizes))
+        allt = np.concatenate([np.asarray(_host(c)) for c in chunks])
+        out = self.accelerations(allt, theta=theta, softening=softening, G=G)
+        return np.split(out, np.cumsum(sizes)[:-1])
+
     def evaluate_accelerations(self, softening, theta: float = 0.5, G: float = 1.0):
         """bhut/api.py:733-786."""
         if not self._is_built or self._handle is None:
@@ -575,3 +623,38 @@ def direct_accelerations(positions, masses, *, softening: float = 0.0, G: float 
     _lib.check(_lib.load().bhut_direct_accelerations(_ptr(pos), _ptr(m), n, dim, _ptr(tg), mt,
                                                      float(softening), float(G), _ptr(out), None))
     return out
+
+
+def compute_tree_statistics(tree, positions, theta: float = 0.5) -> dict:
+    """bhut/traverse/bh.py:604-700 on the GPU: average nodes visited,
+    particles computed and monopoles used per target, and their total.
+
+    ``tree`` is a TreeData (from ``Tree._tree`` or ``build_tree``) or a built
+    ``Tree``; ``positions`` are the targets (N, dim).  Counting follows the
+    reference exactly: every popped node is a visit, a visited non-empty leaf
+    counts ``count - 1`` particles whether or not the target lies in it, an
+    accepted internal node counts one monopole.
+    """
+    if isinstance(tree, Tree):
+        tree = tree._tree
+        if tree is None:
+            raise RuntimeError("Tree not built. Call build() first.")
+    pos = np.ascontiguousarray(_host(positions), dtype=np.float64)
+    n_particles = len(pos)
+    dim = pos.shape[1] if pos.ndim == 2 else tree.dim
+    i64 = lambda a: np.ascontiguousarray(a, dtype=np.int64)  # noqa: E731
+    arrays = [np.ascontiguousarray(tree.com, dtype=np.float64),
+              np.ascontiguousarray(tree.half_size, dtype=np.float64),
+              np.ascontiguousarray(tree.mass, dtype=np.float64),
+              i64(tree.first_child), i64(tree.child_count), i64(tree.start), i64(tree.count)]
+    totals = np.zeros(3, dtype=np.int64)
+    _lib.check(_lib.load().bhut_tree_statistics(
+        *[a.ctypes.data for a in arrays], len(arrays[2]), int(dim), pos.ctypes.data,
+        n_particles, float(theta), None, totals.ctypes.data))
+    nodes, parts, monos = (int(v) for v in totals)
+    return {
+        "avg_nodes_visited": nodes / n_particles,
+        "avg_particles_computed": parts / n_particles,
+        "avg_monopoles_used": monos / n_particles,
+        "total_operations": parts + monos,
+    }

@@ -747,4 +747,48 @@ int bhut_direct_accelerations(const double* positions, const double* masses, int
     return rc;
 }
 
+int bhut_tree_statistics(const double* com, const double* half_size, const double* mass,
+                         const int64_t* first_child, const int64_t* child_count,
+                         const int64_t* start, const int64_t* count, int64_t num_nodes, int dim,
+                         const double* targets, int64_t nt, double theta, void* stream,
+                         int64_t* totals)
+{
+    if (dim != 2 && dim != 3) { set_error("dim must be 2 or 3, got %d", dim); return kInvalid; }
+    if (num_nodes <= 0 || !totals) { set_error("empty tree"); return kInvalid; }
+    if (nt < 0 || (nt > 0 && !targets)) { set_error("invalid targets"); return kInvalid; }
+    bhut_tree* t = nullptr;
+    BHUT_TRY(bhut_tree_create(dim, 1, stream, &t));
+    cudaStream_t s = t->stream;
+    DevBuf d_com, d_half, d_mass, d_fc, d_cc, d_start, d_count, d_tot;
+    const size_t md = sizeof(double) * num_nodes, mi = sizeof(int64_t) * num_nodes;
+    int rc = stage_in(d_com, com, md * dim, s);
+    if (rc == kOk) rc = stage_in(d_half, half_size, md, s);
+    if (rc == kOk) rc = stage_in(d_mass, mass, md, s);
+    if (rc == kOk) rc = stage_in(d_fc, first_child, mi, s);
+    if (rc == kOk) rc = stage_in(d_cc, child_count, mi, s);
+    if (rc == kOk) rc = stage_in(d_start, start, mi, s);
+    if (rc == kOk) rc = stage_in(d_count, count, mi, s);
+    if (rc == kOk && nt > 0) rc = stage_in(t->tpos, targets, sizeof(double) * nt * dim, s);
+    if (rc == kOk) rc = d_tot.ensure(sizeof(unsigned long long) * 3, s);
+    if (rc == kOk) {
+        StatTree st{d_com.as<double>(), d_half.as<double>(), d_mass.as<double>(),
+                    d_fc.as<int64_t>(), d_cc.as<int64_t>(), d_start.as<int64_t>(),
+                    d_count.as<int64_t>(), num_nodes};
+        rc = launch_tree_statistics(st, dim, t->tpos.as<double>(), nt, theta,
+                                    d_tot.as<unsigned long long>(), t->err.as<unsigned>(), s);
+    }
+    unsigned long long h[3] = {0, 0, 0};
+    if (rc == kOk) {
+        cudaError_t e = cudaMemcpyAsync(h, d_tot.p, sizeof(h), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy totals");
+    }
+    if (rc == kOk) rc = check_err_word(t, "tree statistics");
+    if (rc == kOk)
+        for (int k = 0; k < 3; k++) totals[k] = (int64_t)h[k];
+    for (DevBuf* b : {&d_com, &d_half, &d_mass, &d_fc, &d_cc, &d_start, &d_count, &d_tot})
+        b->release(s);
+    bhut_tree_destroy(t);
+    return rc;
+}
+
 }  // extern "C"

@@ -274,6 +274,81 @@ int launch_traverse_exact(const TreeDev& t, const double* tx, const double* ty, 
     return kOk;
 }
 
+// ---------------------------------------------------------------------------
+// Operation counts of compute_tree_statistics (bhut/traverse/bh.py:604-700)
+// over any TreeData arrays: per target, nodes popped (empty and out-of-range
+// ones included), count - 1 particles for every visited non-empty leaf, and
+// accepted internal nodes; opening test of bh.py:576-601 (open_exact).
+// One thread per target, private stack; totals summed with warp shuffles and
+// one 64-bit atomic per warp and counter.
+// ---------------------------------------------------------------------------
+constexpr int kStatStack = 128;
+
+template <int DIM>
+__global__ void __launch_bounds__(256)
+k_tree_statistics(StatTree t, const double* __restrict__ tg, int64_t nt, double theta,
+                  unsigned long long* __restrict__ totals, unsigned* __restrict__ err)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    unsigned long long nodes = 0, parts = 0, monos = 0;
+    if (i < nt) {
+        const double x = tg[i * DIM], y = tg[i * DIM + 1], z = DIM == 3 ? tg[i * DIM + 2] : 0.0;
+        int64_t stack[kStatStack];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            const int64_t k = stack[--sp];
+            nodes++;
+            if (k < 0 || k >= t.m || t.mass[k] == 0.0) continue;
+            const int64_t fc = t.first_child[k];
+            if (fc == -1) {
+                const int64_t c = t.count[k];
+                if (t.start[k] != -1 && c > 0) parts += (unsigned long long)(c - 1);
+                continue;
+            }
+            NodeCM cm;
+            cm.x = t.com[k * DIM];
+            cm.y = t.com[k * DIM + 1];
+            cm.z = DIM == 3 ? t.com[k * DIM + 2] : 0.0;
+            cm.w = 0.0;
+            if (open_exact<DIM>(x, y, z, cm, __dmul_rn(2.0, t.half_size[k]), theta)) {
+                const int64_t nc = t.child_count[k];
+                if (sp + nc > kStatStack) {
+                    atomicOr(err, kErrStackOverflow);
+                    break;
+                }
+                for (int64_t j = 0; j < nc; j++) stack[sp++] = fc + j;
+            } else {
+                monos++;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        nodes += __shfl_down_sync(0xffffffffu, nodes, o);
+        parts += __shfl_down_sync(0xffffffffu, parts, o);
+        monos += __shfl_down_sync(0xffffffffu, monos, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&totals[0], nodes);
+        atomicAdd(&totals[1], parts);
+        atomicAdd(&totals[2], monos);
+    }
+}
+
+int launch_tree_statistics(const StatTree& t, int dim, const double* targets, int64_t nt,
+                           double theta, unsigned long long* totals, unsigned* err,
+                           cudaStream_t s)
+{
+    BHUT_CUDA(cudaMemsetAsync(totals, 0, sizeof(unsigned long long) * 3, s));
+    if (nt <= 0) return kOk;
+    const unsigned grid = (unsigned)((nt + 255) / 256);
+    if (dim == 3) k_tree_statistics<3><<<grid, 256, 0, s>>>(t, targets, nt, theta, totals, err);
+    else k_tree_statistics<2><<<grid, 256, 0, s>>>(t, targets, nt, theta, totals, err);
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
+    return kOk;
+}
+
 int direct_chunks(int64_t n, int64_t nt)
 {
     const int64_t tblocks = (nt + kDirectThreads - 1) / kDirectThreads;

@@ -164,6 +164,22 @@ int launch_traverse_fast(const TreeDev& t, const FastTree& ft, const float4* th,
                          const int32_t* self_id, const int32_t* out_idx, int64_t nt, double theta,
                          double eps, double G, double eps_scaled_sq, double* out, unsigned* err,
                          unsigned long long* stats, cudaStream_t s, bool fp32, int mac);
+// TreeData arrays as the reference lays them out (bhut/tree/node.py:15-77):
+// int64 indices, com (m, dim), for compute_tree_statistics.
+struct StatTree {
+    const double* com;
+    const double* half_size;
+    const double* mass;
+    const int64_t* first_child;
+    const int64_t* child_count;
+    const int64_t* start;
+    const int64_t* count;
+    int64_t m;
+};
+int launch_tree_statistics(const StatTree& t, int dim, const double* targets, int64_t nt,
+                           double theta, unsigned long long* totals, unsigned* err,
+                           cudaStream_t s);
+
 int direct_chunks(int64_t n, int64_t nt);
 int launch_direct(const double* pos, const double* mass, int64_t n, int dim, const double* targets,
                   const int64_t* self_id, int64_t nt, double eps, double G, double* out,

@@ -2,7 +2,7 @@
 
     python -m bhut_gb300.reports precision [--n 4000000] [--sample 8192]
     python -m bhut_gb300.reports batched [--nsys 2048]
-    python -m bhut_gb300.reports served [--count 24]
+    python -m bhut_gb300.reports served [--count 24] [--theta 0.7]
 
 ``precision``: the galaxy model (70 % exponential disc, 30 % Hernquist bulge,
 equal masses), softening 0.005, theta in {0.3, 0.5, 0.7}.  For each theta the
@@ -175,49 +175,60 @@ def batched_report(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: i
 
 
 def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: int = 21,
-                  plain_seconds: float = 90.0, err_requests: int = 4,
-                  criterion: str = "bh_offset", multipole: str = "mono"):
+                  plain_seconds: float = 90.0, err_requests: int = 6, theta: float = 0.7,
+                  criterion: str = "bh_offset", multipole: str = "quad",
+                  plain_theta: float = 0.5):
     """``served``: a Poisson stream (mean ``rate`` requests/s) of ``count``
     systems (N log-uniform in [1e3, 2e6], half Plummer, half uniform cubes of
     side 2, velocities N(0, 0.1^2)), each advanced ``steps`` KDK steps
-    (dt = 1e-3, theta = 0.5, eps = 0.01), refit every step, rebuild every 10;
-    the continuous-batching server (FP32 form, offset criterion) against the
-    plain per-request path (form fast, reference criterion), both in real
-    time from the same arrival schedule; latencies include queueing.  Errors
-    vs FP64 direct sum on the initial conditions of a few requests."""
+    (dt = 1e-3, eps = 0.01), refit every step, rebuild every 10; the
+    continuous-batching server (FP32 form; by default theta 0.7, offset
+    criterion, quadrupoles) against the plain per-request path (form fast,
+    the reference's monopole/theta 0.5 configuration), both in real time from
+    the same arrival schedule; latencies include queueing.  Median errors vs
+    FP64 direct sum on the initial conditions of requests spread over the
+    size range, for both configurations."""
     from . import serve
     reqs = serve.request_stream(count, rate=rate, steps=steps, seed=seed)
     total_n = sum(r.n for r in reqs)
-    _log(f"{count} requests, {total_n:,} particles, offered "
-         f"{rate * steps * total_n / count:.3g} accels/s")
-    # accuracy of both configurations on initial conditions
+    _log(f"{count} requests, {total_n:,} particles")
     errs_srv, errs_plain = [], []
-    for r in sorted(reqs, key=lambda r: r.n)[:err_requests]:
+    by_size = sorted(reqs, key=lambda r: r.n)
+    pick = [by_size[int(round(k))] for k in np.linspace(0, len(by_size) - 1, err_requests)]
+    for r in pick:
         idx = precision.sample_indices(r.n, 2048, seed=1)
         ref = precision.direct_reference(r.positions, r.masses, idx, softening=0.01)
-        a_s = api.accelerations(r.positions, r.masses, theta=0.5, softening=0.01,
+        a_s = api.accelerations(r.positions, r.masses, theta=theta, softening=0.01,
                                 form="fp32", criterion=criterion, multipole=multipole,
                                 leaf_size=16)
-        a_p = api.accelerations(r.positions, r.masses, theta=0.5, softening=0.01, form="fast")
+        a_p = api.accelerations(r.positions, r.masses, theta=plain_theta, softening=0.01,
+                                form="fast")
         errs_srv.append(precision.error_distribution(a_s[idx], ref)["median"])
         errs_plain.append(precision.error_distribution(a_p[idx], ref)["median"])
     _log(f"median errors: served {errs_srv}, plain {errs_plain}")
-    sv = serve.Server(theta=0.5, softening=0.01, dt=1e-3, rebuild_every=10, form="fp32",
+    sv = serve.Server(theta=theta, softening=0.01, dt=1e-3, rebuild_every=10, form="fp32",
                       criterion=criterion, multipole=multipole)
     st = sv.run(reqs, realtime=True)
     sv.close()
     _log(f"served: {st}")
     reqs2 = serve.request_stream(count, rate=rate, steps=steps, seed=seed)
-    pl = serve.plain_path(reqs2, theta=0.5, softening=0.01, dt=1e-3, rebuild_every=10,
+    pl = serve.plain_path(reqs2, theta=plain_theta, softening=0.01, dt=1e-3, rebuild_every=10,
                           realtime=True, max_seconds=plain_seconds)
     _log(f"plain: {pl}")
     line = {"report": "served", "requests": count, "rate_per_s": rate, "steps": steps,
-            "particles": total_n, "criterion": criterion, "multipole": multipole,
+            "particles": total_n,
+            "served_config": {"form": "fp32", "theta": theta, "criterion": criterion,
+                              "multipole": multipole, "leaf_size": 16},
+            "plain_config": {"form": "fast", "theta": plain_theta, "criterion": "bh",
+                             "multipole": "mono", "leaf_size": 32},
             "served": st, "plain": pl,
             "solves_per_s_ratio": st["solves_per_s"] / pl["solves_per_s"]
             if pl["solves_per_s"] else None,
-            "median_err_vs_direct": {"served_fp32": float(np.median(errs_srv)),
-                                     "plain_fast_bh": float(np.median(errs_plain))}}
+            "err_requests_n": [r.n for r in pick],
+            "median_err_vs_direct": {"served": float(np.median(errs_srv)),
+                                     "plain": float(np.median(errs_plain)),
+                                     "served_per_request": errs_srv,
+                                     "plain_per_request": errs_plain}}
     print(json.dumps(line), flush=True)
     return line
 
@@ -230,18 +241,22 @@ def main():
     ap.add_argument("--n", type=int, default=4_000_000)
     ap.add_argument("--sample", type=int, default=8192)
     ap.add_argument("--criterion", default=None)
-    ap.add_argument("--multipole", default="mono")
+    ap.add_argument("--multipole", default=None)
+    ap.add_argument("--theta", type=float, default=None)
     ap.add_argument("--thetas", default="0.3,0.5,0.7")
     args = ap.parse_args()
     if args.report == "precision":
         precision_report(args.n, args.sample, criterion=args.criterion or "bh",
-                         multipole=args.multipole,
+                         multipole=args.multipole or "mono",
                          thetas=tuple(float(x) for x in args.thetas.split(",")))
     elif args.report == "batched":
-        batched_report(args.nsys, criterion=args.criterion or "bh", multipole=args.multipole)
+        batched_report(args.nsys, criterion=args.criterion or "bh",
+                       multipole=args.multipole or "mono",
+                       theta=args.theta if args.theta is not None else 0.5)
     elif args.report == "served":
         served_report(args.count, criterion=args.criterion or "bh_offset",
-                      multipole=args.multipole)
+                      multipole=args.multipole or "quad",
+                      theta=args.theta if args.theta is not None else 0.7)
 
 
 if __name__ == "__main__":

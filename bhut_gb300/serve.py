@@ -106,7 +106,7 @@ class Server:
                  dt: float = 1e-3, rebuild_every: int = 10, form: str = "fp32",
                  criterion: str = "bh_offset", leaf_size: int = 16, targets_per_warp: int = 32,
                  hbm_budget: float = 150e9, max_active_particles: int | None = None,
-                 multipole: str = "mono"):
+                 multipole: str = "quad"):
         import torch
         self.torch = torch
         self.theta, self.eps, self.G, self.dt = theta, softening, G, dt

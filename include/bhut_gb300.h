@@ -214,6 +214,17 @@ BHUT_API int bhut_direct_accelerations(const double *positions, const double *ma
                               const double *targets, int64_t m, double softening, double G,
                               double *out, void *stream);
 
+/* Operation counts of compute_tree_statistics (bhut/traverse/bh.py:604-700)
+ * for any TreeData arrays (host or device pointers; int64 indices, com as
+ * (num_nodes, dim)): totals[0] = nodes visited, totals[1] = particles
+ * computed, totals[2] = monopoles used, summed over the nt targets (the
+ * reference divides by the target count for its averages). */
+BHUT_API int bhut_tree_statistics(const double *com, const double *half_size, const double *mass,
+                                  const int64_t *first_child, const int64_t *child_count,
+                                  const int64_t *start, const int64_t *count, int64_t num_nodes,
+                                  int dim, const double *targets, int64_t nt, double theta,
+                                  void *stream, int64_t *totals);
+
 #ifdef __cplusplus
 }
 #endif

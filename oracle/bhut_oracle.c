@@ -529,6 +529,54 @@ EXPORT void bo_accel(const double *com, const double *half_size, const double *m
     (void)nthreads;
 }
 
+/* Operation counts of compute_tree_statistics (bh.py:604-700): for each
+ * target, the nodes popped (empty and out-of-range ones included), the
+ * particles of every visited non-empty leaf minus one (count - 1, whether or
+ * not the target lies in that leaf) and the accepted internal nodes, with the
+ * opening test of bh.py:576-601.  totals = (nodes_visited,
+ * particles_computed, monopoles_used) summed over the targets. */
+EXPORT int bo_tree_statistics(const double *com, const double *half_size, const double *mass,
+                              const int64_t *first_child, const int64_t *child_count,
+                              const int64_t *start, const int64_t *count, int64_t num_nodes,
+                              int dim, const double *targets, int64_t nt, double theta,
+                              int64_t *totals, int nthreads)
+{
+    int64_t nodes = 0, parts = 0, monos = 0;
+    int bad = 0;
+    (void)nthreads;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads) \
+    reduction(+ : nodes, parts, monos, bad)
+#endif
+    for (int64_t i = 0; i < nt; i++) {
+        const double *x = targets + i * dim;
+        int64_t stack[512];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            int64_t k = stack[--sp];
+            nodes++;
+            if (k < 0 || k >= num_nodes || mass[k] == 0) continue;
+            if (first_child[k] == -1) {
+                if (start[k] != -1 && count[k] > 0) parts += count[k] - 1;
+            } else if (should_open(x, com + k * dim, 2 * half_size[k], theta, dim)) {
+                int64_t ch = first_child[k];
+                for (int64_t j = 0; j < child_count[k]; j++) {
+                    if (sp >= 512) { bad++; sp = 0; break; }
+                    stack[sp++] = ch + j;
+                }
+            } else {
+                monos++;
+            }
+        }
+    }
+    totals[0] = nodes;
+    totals[1] = parts;
+    totals[2] = monos;
+    return bad ? -1 : 0;
+}
+
 /* FP64 direct sum over all sources (the theta = 0 limit, bh.py:226-280
  * arithmetic).  self_idx as in bo_accel. */
 EXPORT void bo_direct(const double *pos, const double *m, int64_t n, int dim,

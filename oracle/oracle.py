@@ -65,6 +65,10 @@ def lib():
                                ctypes.c_int]
         L.bo_direct.argtypes = [_D, _D, ctypes.c_int64, ctypes.c_int, _D, ctypes.c_int64, _I64,
                                 ctypes.c_double, ctypes.c_double, _D, ctypes.c_int]
+        L.bo_tree_statistics.restype = ctypes.c_int
+        L.bo_tree_statistics.argtypes = [_D, _D, _D, _I64, _I64, _I64, _I64, ctypes.c_int64,
+                                         ctypes.c_int, _D, ctypes.c_int64, ctypes.c_double,
+                                         _I64, ctypes.c_int]
         L.bo_num_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -245,6 +249,25 @@ def direct_sum(pos: np.ndarray, masses: np.ndarray, *, softening: float, G: floa
     lib().bo_direct(_p(pos, _D), _p(masses, _D), n, dim, _p(tg, _D), nt, _p(idx, _I64),
                     float(softening), float(G), _p(out, _D), int(nthreads))
     return out
+
+
+def tree_statistics(tree, targets: np.ndarray, theta: float = 0.5, nthreads: int = 0):
+    """Totals (nodes_visited, particles_computed, monopoles_used) of
+    compute_tree_statistics (bh.py:604-700) over ``targets``; ``tree`` is
+    any object with the TreeData arrays."""
+    tg = _f64(targets)
+    i64 = lambda a: np.ascontiguousarray(a, dtype=np.int64)  # noqa: E731
+    tot = np.zeros(3, np.int64)
+    com = _f64(tree.com)
+    rc = lib().bo_tree_statistics(_p(com, _D), _p(_f64(tree.half_size), _D),
+                                  _p(_f64(tree.mass), _D), _p(i64(tree.first_child), _I64),
+                                  _p(i64(tree.child_count), _I64), _p(i64(tree.start), _I64),
+                                  _p(i64(tree.count), _I64), len(tree.mass), tg.shape[1],
+                                  _p(tg, _D), tg.shape[0], float(theta), _p(tot, _I64),
+                                  int(nthreads))
+    if rc != 0:
+        raise RuntimeError("tree statistics: traversal stack overflow")
+    return tuple(int(v) for v in tot)
 
 
 def num_threads() -> int:

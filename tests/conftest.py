@@ -55,6 +55,11 @@ def golden_plummer():
     return load_golden("plummer1m_digest")
 
 
+@pytest.fixture(scope="session")
+def golden_stats():
+    return load_golden("tree_statistics")
+
+
 TREE_FIELDS = ["center", "half_size", "mass", "com", "first_child", "child_count", "start",
                "count", "is_leaf", "perm"]
 

@@ -204,10 +204,38 @@ def case_plummer_1m():
          digest_values=np.array(list(digests.values())))
 
 
+def case_statistics():
+    """compute_tree_statistics (bh.py:604-700) of the reference on its own
+    trees: a 3,000-particle Gaussian (L=32 and L=8, theta 0.5 and 0.9), a
+    2-D case, and small systems with zero masses and duplicates."""
+    from bhut.traverse.bh import compute_tree_statistics
+    out = {}
+    rng = np.random.default_rng(23)
+    cases = {"gauss3k": (rng.standard_normal((3000, 3)), np.ones(3000)),
+             "gauss2d_1k": (rng.standard_normal((1000, 2)), rng.uniform(0.5, 2.0, 1000))}
+    small = small_systems()
+    for k in ("zero_masses_n50", "duplicates_n20", "normal_n1", "all_zero_mass_n9"):
+        cases[k] = small[k]
+    names = []
+    for name, (pos, m) in cases.items():
+        out[f"{name}__pos"] = pos
+        out[f"{name}__masses"] = m
+        for L in (32, 8):
+            t = ref_tree(pos, m, L)
+            for theta in (0.5, 0.9):
+                st = compute_tree_statistics(t, pos, theta)
+                tag = f"{name}__L{L}__t{theta}"
+                names.append(tag)
+                out[tag] = np.array([st["avg_nodes_visited"], st["avg_particles_computed"],
+                                     st["avg_monopoles_used"], st["total_operations"]])
+    out["names"] = np.array(names)
+    save("tree_statistics", **out)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["gauss10k", "small", "refit", "plummer1m"]
+    which = sys.argv[1:] or ["gauss10k", "small", "refit", "plummer1m", "statistics"]
     for w in which:
         t0 = time.time()
         {"gauss10k": case_gauss10k, "small": case_small, "refit": case_refit,
-         "plummer1m": case_plummer_1m}[w]()
+         "plummer1m": case_plummer_1m, "statistics": case_statistics}[w]()
         print(f"{w}: {time.time() - t0:.1f} s")

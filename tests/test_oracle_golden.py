@@ -119,3 +119,24 @@ def test_known_answers(oracle_mod):
     t = oracle_mod.build_tree(pos, m, 32)
     a = oracle_mod.accelerations(t, pos, m, theta=0.5, softening=0.0)
     np.testing.assert_allclose(np.linalg.norm(a, axis=1), 1e-12, rtol=1e-10)
+
+
+def stats_cases(g):
+    """(tag, positions, masses, leaf_size, theta, reference values) of the
+    compute_tree_statistics fixture."""
+    for tag in g["names"]:
+        name, L, t = str(tag).split("__")
+        yield (str(tag), g[f"{name}__pos"], g[f"{name}__masses"], int(L[1:]), float(t[1:]),
+               g[str(tag)])
+
+
+def test_tree_statistics(oracle_mod, golden_stats):
+    n_cases = 0
+    for tag, pos, m, L, theta, want in stats_cases(golden_stats):
+        t = oracle_mod.build_tree(pos, m, L)
+        nodes, parts, monos = oracle_mod.tree_statistics(t, pos, theta)
+        n = len(pos)
+        got = np.array([nodes / n, parts / n, monos / n, parts + monos])
+        assert np.array_equal(got, want), (tag, got, want)
+        n_cases += 1
+    assert n_cases == 24
