@@ -227,6 +227,10 @@ def measure_gemm_peak(torch, dtype) -> float:
 # rsqrt and cube 11, m * w 4, three float-float products and accumulations
 # 36 -> 107 (plus one MUFU rsqrt).
 FF_OPS_PER_INTERACTION = 107
+# ... and of one FP32/Kahan pair term of the fp32 form (pair_f32, fast.cuh):
+# displacement 9, r^2 + eps^2 3, check 1, cube 2, m * w 1, three Kahan
+# products and additions 15 -> 31 (plus one MUFU rsqrt).
+F32_OPS_PER_INTERACTION = 31
 
 
 def run_ours(args, ws, rank, local):
@@ -318,17 +322,20 @@ def run_ours(args, ws, rank, local):
             "work_rule": f"{FLOPS_PER_INTERACTION} flop x (pair + monopole evaluations counted "
                          "by the kernel)"}
     else:
-        ops = FF_OPS_PER_INTERACTION * inter
+        per = FF_OPS_PER_INTERACTION if args.form == "fast" else F32_OPS_PER_INTERACTION
+        ops = per * inter
         achieved32 = ops / trav_s / 1e12
         fma_rate = peak32 / 2.0      # FP32 pipe lane-instructions per second (one FMA = 2 flop)
         roofline = {
-            "bound": "fp32", "kernel": "k_traverse_fast", "achieved": achieved32,
+            "bound": "fp32",
+            "kernel": "k_traverse_fast" if args.form == "fast" else "k_traverse_fp32",
+            "achieved": achieved32,
             "peak": fma_rate, "unit": "T FP32-pipe ops/s", "frac": achieved32 / fma_rate,
             "traffic": traffic,
             "peak_source": "cuBLAS SGEMM 4096^3 (TF32 off) measured in this run, / 2 for the "
                            "FMA-instruction rate (MEASURED_PEAKS.json has no FP32 figure)",
             "work_per_launch": ops,
-            "work_rule": f"{FF_OPS_PER_INTERACTION} FP32 ops per float-float pair/monopole term "
+            "work_rule": f"{per} FP32 ops per pair/monopole term of form {args.form} "
                          "x evaluations counted by the kernel",
             "fp64_equivalent": {"achieved": achieved64, "peak": peak64, "unit": "TFLOP/s",
                                 "frac": achieved64 / peak64,
@@ -350,6 +357,8 @@ def run_ours(args, ws, rank, local):
                                    "fp64_fallback_decisions": fb_dec, "fp64_pairs": fb_pairs},
         "clocks": clk,
     }
+    if ws == 1 and not args.no_served:
+        line["served"] = served_summary(args)
     if not args.no_cpu_baseline:
         cb = cpu_solve_sample(pos, m, args.cpu_sample)
         line["cpu_baseline"] = {
@@ -360,6 +369,30 @@ def run_ours(args, ws, rank, local):
                       f"{cb['cores']} threads), extrapolated to N targets"}
     h.close()
     print(json.dumps(line), flush=True)
+
+
+def served_summary(args) -> dict:
+    """The served half of the metric: the continuous-batching server against
+    the plain per-request GPU path on the same Poisson stream (24 systems,
+    N log-uniform in [1e3, 2e6], 100 KDK steps each, 200 requests/s), with
+    both configurations' median error vs FP64 direct sum."""
+    from bhut_gb300 import reports
+    r = reports.served_report(count=args.served_count, plain_seconds=args.served_plain_seconds,
+                              closed_loop=False, emit=False)
+    sv, pl = r["served"], r["plain"]
+    return {
+        "workload": f"{r['requests']} requests, {r['particles']:,} particles, Poisson "
+                    f"{r['rate_per_s']:.0f}/s, {r['steps']} KDK steps each, refit every step, "
+                    "rebuild every 10",
+        "served_config": r["served_config"], "plain_config": r["plain_config"],
+        "solves_per_s": sv["solves_per_s"], "latency_p50_s": sv["latency_p50_s"],
+        "latency_p99_s": sv["latency_p99_s"], "plain_solves_per_s": pl["solves_per_s"],
+        "plain_latency_p50_s": pl["latency_p50_s"], "plain_latency_p99_s": pl["latency_p99_s"],
+        "plain_requests_done": pl["requests_done"],
+        "solves_per_s_ratio": r["solves_per_s_ratio"],
+        "median_err_vs_fp64_direct": {"served": r["median_err_vs_direct"]["served"],
+                                      "plain": r["median_err_vs_direct"]["plain"]},
+    }
 
 
 def _traffic_from_profile(args):
@@ -384,6 +417,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--ref-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-served", action="store_true",
+                    help="skip the served-stream comparison (about a minute)")
+    ap.add_argument("--served-count", type=int, default=24)
+    ap.add_argument("--served-plain-seconds", type=float, default=60.0)
     args = ap.parse_args()
     if args.form is None:
         from bhut_gb300.api import DEFAULT_FORM

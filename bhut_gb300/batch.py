@@ -176,3 +176,57 @@ def autotune(positions, masses, offsets, *, theta: float, softening: float, G: f
             times[(L, tpw)] = best
     best = min(times, key=times.get)
     return {"leaf_size": best[0], "targets_per_warp": best[1]}, times
+
+
+def main():
+    """Times the batched solver on seeded Plummer systems:
+
+        python -m bhut_gb300.batch [--nsys 2048] [--nmin 256] [--nmax 65536]
+            [--leaf 16] [--tpw 32] [--form fp32] [--multipole mono] [--solves 3]
+
+    prints one JSON line (ms per solve, systems/s, accels/s)."""
+    import argparse
+    import json
+
+    import torch
+
+    from . import workloads
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--nsys", type=int, default=2048)
+    ap.add_argument("--nmin", type=int, default=256)
+    ap.add_argument("--nmax", type=int, default=65536)
+    ap.add_argument("--leaf", type=int, default=16)
+    ap.add_argument("--tpw", type=int, default=32)
+    ap.add_argument("--form", default="fp32")
+    ap.add_argument("--criterion", default="bh")
+    ap.add_argument("--multipole", default="mono")
+    ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--softening", type=float, default=0.01)
+    ap.add_argument("--solves", type=int, default=3)
+    ap.add_argument("--seed", type=int, default=11)
+    a = ap.parse_args()
+    pos, m, off = concat_systems(workloads.plummer_batch(a.nsys, a.nmin, a.nmax, seed=a.seed))
+    pd, md = torch.as_tensor(pos).cuda(), torch.as_tensor(m).cuda()
+    sv = BatchedSolver(leaf_size=a.leaf, form=a.form, criterion=a.criterion,
+                       targets_per_warp=a.tpw, use_graph=True, multipole=a.multipole)
+    sv.load(pd, md, off)
+    out = torch.empty_like(pd)
+    sv.solve(theta=a.theta, softening=a.softening, out=out)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(a.solves):
+        sv.solve(theta=a.theta, softening=a.softening, out=out)
+    ev1.record()
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / a.solves
+    p2p, m2p, visits = sv.stats()
+    sv.close()
+    print(json.dumps({"systems": a.nsys, "particles": int(off[-1]), "ms_per_solve": ms,
+                      "systems_per_s": a.nsys / ms * 1e3, "accels_per_s": off[-1] / ms * 1e3,
+                      "p2p": p2p, "m2p": m2p, "visits": visits, "leaf": a.leaf, "tpw": a.tpw,
+                      "form": a.form, "multipole": a.multipole}), flush=True)
+
+
+if __name__ == "__main__":
+    main()

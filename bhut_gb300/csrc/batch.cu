@@ -373,7 +373,7 @@ k_batch_traverse(BatchDev b, BatchArgs a)
             const int node = e.x;
             const bool act = ((unsigned)e.y >> lane) & 1u;
             cnt[2] += act && sub == 0;
-            if ((__double_as_longlong(__ldg(&t.cm[node].w)) << 1) == 0) continue;
+            if (mass_is_zero(t.cm + node)) continue;
             const int fc = t.first_child[node];
             if (fc < 0) {
                 const int s0 = t.start[node], c = t.count[node];

@@ -68,6 +68,22 @@ static __device__ __forceinline__ float two_sum_err(float a, float b, float s)
     return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// mass == +-0 of a node, with 32-bit integer operations on the two words.
+static __device__ __forceinline__ bool mass_is_zero(const NodeCM* c)
+{
+    const int2 w = __ldg(reinterpret_cast<const int2*>(&c->w));
+    return ((w.y & 0x7fffffff) | w.x) == 0;
+}
+
+// MUFU reciprocal square root, flush-to-zero (one instruction; callers pass
+// normal, positive arguments only).
+static __device__ __forceinline__ float rsqrt_mufu(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 static __device__ __forceinline__ float comp(const float4& v, int k)
 {
     return k == 0 ? v.x : (k == 1 ? v.y : v.z);
@@ -123,7 +139,7 @@ __device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4
     }
     // w = R^(-3/2): y ~ R^(-1/2); e = 1 - R y^2 exactly enough;
     // w = y^3 (1 - e)^(-3/2) = y^3 (1 + 3e/2 + 15e^2/8 + O(e^3))
-    const float y = rsqrtf(Rh);
+    const float y = rsqrt_mufu(Rh);                  // Rh >= kTinyR: normal
     const float Y = __fmul_rn(y, y);
     const float Ye = __fmaf_rn(y, y, -Y);
     const float e = -__fmaf_rn(Rh, Ye, __fmaf_rn(Rl, Y, __fmaf_rn(Rh, Y, -1.0f)));
@@ -197,13 +213,16 @@ __device__ __forceinline__ void pair_f32(const float* Th, const float* Tl, float
     const float d2 = DIM == 3 ? __fadd_rn(__fsub_rn(sh.z, Th[2]), __fsub_rn(sl.z, Tl[2])) : 0.0f;
     float r2 = fmaf(d1, d1, fmaf(d0, d0, e2));
     if (DIM == 3) r2 = fmaf(d2, d2, r2);
-    if (!(r2 > 0.0f)) return;                  // r^2 + eps^2 == 0: no term (kernels.py:62-63)
-    const float ri = rsqrtf(r2);
+    // r^2 + eps^2 == 0: no term (kernels.py:62-63); below the normal range
+    // (closer than 2^-63 box sizes, unsoftened) the FP32 force would overflow:
+    // no term either
+    if (!(r2 >= 0x1p-126f)) return;
+    const float ri = rsqrt_mufu(r2);
     const float f = sh.w * (ri * ri * ri);
     const float d[3] = {d0, d1, d2};
 #pragma unroll
     for (int k = 0; k < DIM; k++) {            // Kahan compensated sum
-        const float y = __fsub_rn(__fmul_rn(f, d[k]), cmp[k]);
+        const float y = fmaf(f, d[k], -cmp[k]);
         const float t = __fadd_rn(acc[k], y);
         cmp[k] = __fsub_rn(__fsub_rn(t, acc[k]), y);
         acc[k] = t;
@@ -226,8 +245,8 @@ __device__ __forceinline__ void node_quad_f32(const float* Th, const float* Tl, 
     const float d2 = DIM == 3 ? __fadd_rn(__fsub_rn(nh.z, Th[2]), __fsub_rn(nl.z, Tl[2])) : 0.0f;
     float r2 = fmaf(d1, d1, fmaf(d0, d0, e2));
     if (DIM == 3) r2 = fmaf(d2, d2, r2);
-    if (!(r2 > 0.0f)) return;
-    const float ri = rsqrtf(r2);
+    if (!(r2 >= 0x1p-126f)) return;
+    const float ri = rsqrt_mufu(r2);
     const float ri2 = ri * ri;
     const float ri3 = ri2 * ri;
     const float ri5 = ri3 * ri2;

@@ -171,7 +171,7 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
         const bool act = (mask >> lane) & 1u;
         cnt[2] += act;
         // mass == 0 skip (bh.py:514), tested on the bits: +-0.0 only
-        if ((__double_as_longlong(__ldg(&t.cm[node].w)) << 1) == 0) continue;
+        if (mass_is_zero(t.cm + node)) continue;
         const int fc = t.first_child[node];
         if (fc < 0) {
             const int s = t.start[node], c = t.count[node];
@@ -348,7 +348,7 @@ __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, c
         const unsigned mask = (unsigned)e.y;
         const bool act = (mask >> lane) & 1u;
         cnt[2] += act;
-        if ((__double_as_longlong(__ldg(&t.cm[node].w)) << 1) == 0) continue;
+        if (mass_is_zero(t.cm + node)) continue;
         const int fc = t.first_child[node];
         if (fc < 0) {
             const int s = t.start[node], c = t.count[node];

@@ -177,7 +177,7 @@ def batched_report(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: i
 def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: int = 21,
                   plain_seconds: float = 90.0, err_requests: int = 6, theta: float = 0.7,
                   criterion: str = "bh_offset", multipole: str = "quad",
-                  plain_theta: float = 0.5):
+                  plain_theta: float = 0.5, closed_loop: bool = True, emit: bool = True):
     """``served``: a Poisson stream (mean ``rate`` requests/s) of ``count``
     systems (N log-uniform in [1e3, 2e6], half Plummer, half uniform cubes of
     side 2, velocities N(0, 0.1^2)), each advanced ``steps`` KDK steps
@@ -185,9 +185,11 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
     continuous-batching server (FP32 form; by default theta 0.7, offset
     criterion, quadrupoles) against the plain per-request path (form fast,
     the reference's monopole/theta 0.5 configuration), both in real time from
-    the same arrival schedule; latencies include queueing.  Median errors vs
-    FP64 direct sum on the initial conditions of requests spread over the
-    size range, for both configurations."""
+    the same arrival schedule; latencies include queueing.  With
+    ``closed_loop`` the server also runs the stream saturated (every request
+    queued at t = 0).  Median errors vs FP64 direct sum on the initial
+    conditions of requests spread over the size range, for both
+    configurations."""
     from . import serve
     reqs = serve.request_stream(count, rate=rate, steps=steps, seed=seed)
     total_n = sum(r.n for r in reqs)
@@ -211,6 +213,14 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
     st = sv.run(reqs, realtime=True)
     sv.close()
     _log(f"served: {st}")
+    closed = None
+    if closed_loop:
+        sv = serve.Server(theta=theta, softening=0.01, dt=1e-3, rebuild_every=10, form="fp32",
+                          criterion=criterion, multipole=multipole)
+        closed = sv.run(serve.request_stream(count, rate=rate, steps=steps, seed=seed),
+                        realtime=False)
+        sv.close()
+        _log(f"served, closed loop: {closed}")
     reqs2 = serve.request_stream(count, rate=rate, steps=steps, seed=seed)
     pl = serve.plain_path(reqs2, theta=plain_theta, softening=0.01, dt=1e-3, rebuild_every=10,
                           realtime=True, max_seconds=plain_seconds)
@@ -221,7 +231,7 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
                               "multipole": multipole, "leaf_size": 16},
             "plain_config": {"form": "fast", "theta": plain_theta, "criterion": "bh",
                              "multipole": "mono", "leaf_size": 32},
-            "served": st, "plain": pl,
+            "served": st, "served_closed_loop": closed, "plain": pl,
             "solves_per_s_ratio": st["solves_per_s"] / pl["solves_per_s"]
             if pl["solves_per_s"] else None,
             "err_requests_n": [r.n for r in pick],
@@ -229,7 +239,8 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
                                      "plain": float(np.median(errs_plain)),
                                      "served_per_request": errs_srv,
                                      "plain_per_request": errs_plain}}
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
     return line
 
 
