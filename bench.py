@@ -412,7 +412,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--form", choices=["exact", "fast", "fp32"], default=None)
-    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--n", "--particles", dest="n", type=int, default=N_DEFAULT,
+                    help="particles (--particles under torchrun, whose parser takes --n)")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--ref-sample", type=int, default=0)

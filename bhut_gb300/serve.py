@@ -44,6 +44,25 @@ def bytes_per_particle(leaf_size: int) -> float:
     return STATE_BYTES + BATCH_BYTES + 2.0 * NODE_BYTES / leaf_size
 
 
+def admits(resident: int, n_active: int, n: int, *, leaf_size: int, hbm_budget: float,
+           max_active: int | None = None) -> bool:
+    """Admission rule: a request of ``n`` particles joins ``n_active``
+    resident systems holding ``resident`` particles when the estimated device
+    footprint of all of them fits ``hbm_budget`` bytes and, with a cap, the
+    resident particle count stays within ``max_active`` (a request alone on
+    an empty server is always admitted past the cap, never past the budget)."""
+    if max_active is not None and n_active and resident + n > max_active:
+        return False
+    return (resident + n) * bytes_per_particle(leaf_size) <= hbm_budget
+
+
+def keeps_order(primed: bool, has_order: bool, steps_done: int, rebuild_every: int) -> bool:
+    """Refit (keep the last Morton order) unless this system's rebuild is
+    due: its first solve, and every ``rebuild_every`` of its own steps
+    (bhut's Tree.refit / Tree.rebuild schedule of the served workload)."""
+    return primed and has_order and steps_done % rebuild_every != 0
+
+
 @dataclass
 class Request:
     rid: int
@@ -128,10 +147,9 @@ class Server:
 
     # -- device state ------------------------------------------------------
     def _fits(self, r: Request) -> bool:
-        resident = sum(a.n for a in self.active)
-        if self.max_active is not None and self.active and resident + r.n > self.max_active:
-            return False
-        return (resident + r.n) * bytes_per_particle(self.leaf_size) <= self.hbm_budget
+        return admits(sum(a.n for a in self.active), len(self.active), r.n,
+                      leaf_size=self.leaf_size, hbm_budget=self.hbm_budget,
+                      max_active=self.max_active)
 
     def _pack(self):
         """Concatenates the resident systems' state into one set of device
@@ -171,7 +189,7 @@ class Server:
         keep = np.zeros(len(self.active), dtype=np.uint8)
         perm_in = None
         for k, r in enumerate(self.active):         # refit unless a rebuild is due
-            if r.order is not None and r.primed and r.steps_done % self.rebuild_every != 0:
+            if keeps_order(r.primed, r.order is not None, r.steps_done, self.rebuild_every):
                 keep[k] = 1
         if keep.any():
             perm_in = torch.cat([
