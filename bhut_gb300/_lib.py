@@ -29,6 +29,7 @@ MAC_BH = 0
 MAC_OFFSET = 1
 CRITERIA = {"bh": MAC_BH, "bh_offset": MAC_OFFSET}
 MULTIPOLES = {"mono": 0, "quad": 1}
+STACKS = {"shared": 0, "registers": 1}
 
 _VP = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -65,6 +66,7 @@ SIGNATURES = {
     "bhut_batch_create": (_INT, [_INT, _INT, _VP, ctypes.POINTER(_VP)]),
     "bhut_batch_configure": (_INT, [_VP, _INT, _INT, _INT, _INT]),
     "bhut_batch_set_multipole": (_INT, [_VP, _INT]),
+    "bhut_batch_set_stack": (_INT, [_VP, _INT]),
     "bhut_batch_load": (_INT, [_VP, _VP, _VP, _VP, _I64]),
     "bhut_batch_solve": (_INT, [_VP, _D, _D, _D, _VP]),
     "bhut_batch_info": (_INT, [_VP] + [ctypes.POINTER(_I64)] * 4),

@@ -33,7 +33,7 @@ class BatchedSolver:
 
     def __init__(self, *, dim: int = 3, leaf_size: int = 32, form: str = "fp32",
                  criterion: str = "bh", targets_per_warp: int = 32, use_graph: bool = True,
-                 stream: int | None = None, multipole: str = "mono"):
+                 stream: int | None = None, multipole: str = "mono", stack: str = "shared"):
         self.L = _lib.load()
         self.dim = dim
         self.leaf_size = leaf_size
@@ -41,12 +41,13 @@ class BatchedSolver:
         _lib.check(self.L.bhut_batch_create(int(dim), int(leaf_size), stream, ctypes.byref(h)))
         self.h = h
         self.configure(form=form, criterion=criterion, targets_per_warp=targets_per_warp,
-                       use_graph=use_graph, multipole=multipole)
+                       use_graph=use_graph, multipole=multipole, stack=stack)
         self.offsets = None
         self._keep = None
 
     def configure(self, *, form: str = "fp32", criterion: str = "bh", targets_per_warp: int = 32,
-                  use_graph: bool = True, multipole: str = "mono") -> None:
+                  use_graph: bool = True, multipole: str = "mono",
+                  stack: str = "shared") -> None:
         if form not in ("fp32", "fast"):
             raise ValueError(f"the batched solver runs form 'fp32' or 'fast', got {form!r}")
         if criterion not in _lib.CRITERIA:
@@ -59,7 +60,10 @@ class BatchedSolver:
             raise ValueError(f"multipole must be 'mono', got '{multipole}' "
                          "(form='fp32' also accepts 'quad')")
         _lib.check(self.L.bhut_batch_set_multipole(self.h, _lib.MULTIPOLES[multipole]))
-        self.form, self.criterion, self.multipole = form, criterion, multipole
+        if stack not in _lib.STACKS:
+            raise ValueError(f"stack must be one of {sorted(_lib.STACKS)}, got {stack!r}")
+        _lib.check(self.L.bhut_batch_set_stack(self.h, _lib.STACKS[stack]))
+        self.form, self.criterion, self.multipole, self.stack = form, criterion, multipole, stack
         self.targets_per_warp, self.use_graph = targets_per_warp, use_graph
 
     def load(self, positions, masses, offsets) -> "BatchedSolver":
@@ -145,9 +149,11 @@ def batched_accelerations(systems, *, theta: float = 0.5, softening: float = 0.0
 
 def autotune(positions, masses, offsets, *, theta: float, softening: float, G: float = 1.0,
              form: str = "fp32", criterion: str = "bh", leaf_sizes=(8, 16, 32, 64),
-             targets_per_warp=(32, 16), repeats: int = 2, multipole: str = "mono"):
-    """Times every (leaf_size, targets_per_warp) candidate on this batch
-    (graph replay, warm) and returns (best config, {config: seconds})."""
+             targets_per_warp=(32, 16), stacks=("shared", "registers"), repeats: int = 2,
+             multipole: str = "mono"):
+    """Times every (leaf_size, targets_per_warp, stack placement) candidate on
+    this batch (graph replay, warm) and returns (best config, {config:
+    seconds})."""
     import torch
     pos = _to_f64(positions)
     m = _to_f64(masses)
@@ -156,26 +162,28 @@ def autotune(positions, masses, offsets, *, theta: float, softening: float, G: f
         m = torch.as_tensor(np.asarray(m)).cuda()
     dim = int(pos.shape[1])
     times = {}
+    out = torch.empty((int(offsets[-1]), dim), dtype=torch.float64, device="cuda")
     for L in leaf_sizes:
         for tpw in targets_per_warp:
             if tpw != 32 and dim != 3:
                 continue
-            sv = BatchedSolver(dim=dim, leaf_size=L, form=form, criterion=criterion,
-                               targets_per_warp=tpw, use_graph=True, multipole=multipole)
-            sv.load(pos, m, offsets)
-            out = torch.empty((int(offsets[-1]), dim), dtype=torch.float64, device="cuda")
-            best = float("inf")
-            for r in range(repeats + 1):
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                sv.solve(theta=theta, softening=softening, G=G, out=out)
-                torch.cuda.synchronize()
-                if r:
-                    best = min(best, time.perf_counter() - t0)
-            sv.close()
-            times[(L, tpw)] = best
+            for stk in stacks:
+                sv = BatchedSolver(dim=dim, leaf_size=L, form=form, criterion=criterion,
+                                   targets_per_warp=tpw, use_graph=True, multipole=multipole,
+                                   stack=stk)
+                sv.load(pos, m, offsets)
+                best = float("inf")
+                for r in range(repeats + 1):
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    sv.solve(theta=theta, softening=softening, G=G, out=out)
+                    torch.cuda.synchronize()
+                    if r:
+                        best = min(best, time.perf_counter() - t0)
+                sv.close()
+                times[(L, tpw, stk)] = best
     best = min(times, key=times.get)
-    return {"leaf_size": best[0], "targets_per_warp": best[1]}, times
+    return {"leaf_size": best[0], "targets_per_warp": best[1], "stack": best[2]}, times
 
 
 def main():
@@ -200,6 +208,7 @@ def main():
     ap.add_argument("--form", default="fp32")
     ap.add_argument("--criterion", default="bh")
     ap.add_argument("--multipole", default="mono")
+    ap.add_argument("--stack", default="shared")
     ap.add_argument("--theta", type=float, default=0.5)
     ap.add_argument("--softening", type=float, default=0.01)
     ap.add_argument("--solves", type=int, default=3)
@@ -208,7 +217,8 @@ def main():
     pos, m, off = concat_systems(workloads.plummer_batch(a.nsys, a.nmin, a.nmax, seed=a.seed))
     pd, md = torch.as_tensor(pos).cuda(), torch.as_tensor(m).cuda()
     sv = BatchedSolver(leaf_size=a.leaf, form=a.form, criterion=a.criterion,
-                       targets_per_warp=a.tpw, use_graph=True, multipole=a.multipole)
+                       targets_per_warp=a.tpw, use_graph=True, multipole=a.multipole,
+                       stack=a.stack)
     sv.load(pd, md, off)
     out = torch.empty_like(pd)
     sv.solve(theta=a.theta, softening=a.softening, out=out)
@@ -225,7 +235,7 @@ def main():
     print(json.dumps({"systems": a.nsys, "particles": int(off[-1]), "ms_per_solve": ms,
                       "systems_per_s": a.nsys / ms * 1e3, "accels_per_s": off[-1] / ms * 1e3,
                       "p2p": p2p, "m2p": m2p, "visits": visits, "leaf": a.leaf, "tpw": a.tpw,
-                      "form": a.form, "multipole": a.multipole}), flush=True)
+                      "form": a.form, "multipole": a.multipole, "stack": a.stack}), flush=True)
 
 
 if __name__ == "__main__":

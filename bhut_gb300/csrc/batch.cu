@@ -314,12 +314,87 @@ struct BatchArgs {
     unsigned long long* stats;
 };
 
-template <int DIM, bool FP32, int TPW>
+// The warp's traversal stack of (node, lane mask) entries, two placements:
+//  STK 0: in shared memory, lane 0 writes, every lane reads (one __syncwarp
+//         per pop and per push);
+//  STK 1: in registers, entry j held by lane j % 32 in register j / 32;
+//         a pop is two shuffles from the owning lane, a push a predicated
+//         register write; no shared memory, no __syncwarp.
+// Entries are warp-uniform, so every lane keeps the same depth `sp`.
+template <int STK> struct WarpStack;
+
+template <> struct WarpStack<0> {
+    int2* s;
+    int sp = 0, lane;
+    __device__ WarpStack(int2* s_, int lane_) : s(s_), lane(lane_) {}
+    __device__ void init(int node, unsigned mask)
+    {
+        if (lane == 0) s[0] = make_int2(node, (int)mask);
+        sp = 1;
+        __syncwarp();
+    }
+    __device__ bool empty() const { return sp == 0; }
+    __device__ int2 pop()
+    {
+        const int2 e = s[--sp];
+        __syncwarp();
+        return e;
+    }
+    __device__ bool push2(int fc, unsigned m)
+    {
+        if (sp + 2 > kStackDepth) return false;
+        if (lane == 0) {
+            s[sp] = make_int2(fc, (int)m);
+            s[sp + 1] = make_int2(fc + 1, (int)m);
+        }
+        sp += 2;
+        __syncwarp();
+        return true;
+    }
+};
+
+template <> struct WarpStack<1> {
+    static_assert(kStackDepth <= 2 * kWarp, "register stack holds two entries per lane");
+    int n0 = 0, m0 = 0, n1 = 0, m1 = 0;
+    int sp = 0, lane;
+    __device__ WarpStack(int2*, int lane_) : lane(lane_) {}
+    __device__ void put(int j, int node, int mask)
+    {
+        if (lane == (j & 31)) {
+            if (j < kWarp) { n0 = node; m0 = mask; }
+            else { n1 = node; m1 = mask; }
+        }
+    }
+    __device__ void init(int node, unsigned mask)
+    {
+        put(0, node, (int)mask);
+        sp = 1;
+    }
+    __device__ bool empty() const { return sp == 0; }
+    __device__ int2 pop()
+    {
+        --sp;
+        const bool hi = sp >= kWarp;
+        const int node = __shfl_sync(0xffffffffu, hi ? n1 : n0, sp & 31);
+        const int mask = __shfl_sync(0xffffffffu, hi ? m1 : m0, sp & 31);
+        return make_int2(node, mask);
+    }
+    __device__ bool push2(int fc, unsigned m)
+    {
+        if (sp + 2 > kStackDepth) return false;
+        put(sp, fc, (int)m);
+        put(sp + 1, fc + 1, (int)m);
+        sp += 2;
+        return true;
+    }
+};
+
+template <int DIM, bool FP32, int TPW, int STK>
 __global__ void __launch_bounds__(kBatchThreads)
 k_batch_traverse(BatchDev b, BatchArgs a)
 {
     constexpr int LPT = kWarp / TPW;            // lanes per target
-    __shared__ int2 stack[kBatchWarps][kStackDepth];
+    __shared__ int2 stack[STK == 0 ? kBatchWarps : 1][kStackDepth];
     __shared__ float4 sh[kBatchWarps][kWarp], sl[kBatchWarps][kWarp];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int sub = lane % LPT;
@@ -364,12 +439,10 @@ k_batch_traverse(BatchDev b, BatchArgs a)
         bool overflow = false;
 
         const unsigned live = __ballot_sync(FULL, valid);
-        if (lane == 0) stack[w][0] = make_int2(root, (int)live);
-        int sp = 1;
-        __syncwarp();
-        while (sp > 0) {
-            const int2 e = stack[w][--sp];
-            __syncwarp();
+        WarpStack<STK> st(stack[STK == 0 ? w : 0], lane);
+        st.init(root, live);
+        while (!st.empty()) {
+            const int2 e = st.pop();
             const int node = e.x;
             const bool act = ((unsigned)e.y >> lane) & 1u;
             cnt[2] += act && sub == 0;
@@ -453,14 +526,9 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                     }
                     cnt[1]++;
                 }
-                if (omask) {
-                    if (sp + 2 > kStackDepth) { overflow = true; break; }
-                    if (lane == 0) {
-                        stack[w][sp] = make_int2(fc, (int)omask);
-                        stack[w][sp + 1] = make_int2(fc + 1, (int)omask);
-                    }
-                    sp += 2;
-                    __syncwarp();
+                if (omask && !st.push2(fc, omask)) {
+                    overflow = true;
+                    break;
                 }
             }
         }
@@ -504,6 +572,16 @@ k_batch_traverse(BatchDev b, BatchArgs a)
     }
 }
 
+template <int DIM, bool FP32, int TPW>
+void launch_batch_traverse(int stk, unsigned grid, cudaStream_t s, const BatchDev& bd,
+                           const BatchArgs& a)
+{
+    if (stk == BHUT_STACK_REGISTERS)
+        k_batch_traverse<DIM, FP32, TPW, 1><<<grid, kBatchThreads, 0, s>>>(bd, a);
+    else
+        k_batch_traverse<DIM, FP32, TPW, 0><<<grid, kBatchThreads, 0, s>>>(bd, a);
+}
+
 inline size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
@@ -530,6 +608,7 @@ struct BufB {
 struct bhut_batch {
     int dim = 3, leaf = 32, form = BHUT_FORM_FP32, mac = 0, tpw = 32;
     int multipole = BHUT_MULTIPOLE_MONO;
+    int stack = BHUT_STACK_SHARED;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int64_t nsys = 0, ntot = 0, mtot = 0, ltot = 0;
@@ -751,14 +830,15 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
                 eps, G, b->mac, out, b->err.as<unsigned>(), b->stats.as<unsigned long long>()};
     const unsigned grid = 152u * 6u;   // persistent: about one wave of resident blocks
     const bool fp32 = b->form == BHUT_FORM_FP32;
+    const int stk = b->stack;
     if (dim == 3) {
-        if (fp32 && b->tpw == 32) k_batch_traverse<3, true, 32><<<grid, kBatchThreads, 0, s>>>(bd, a);
-        else if (fp32) k_batch_traverse<3, true, 16><<<grid, kBatchThreads, 0, s>>>(bd, a);
-        else if (b->tpw == 32) k_batch_traverse<3, false, 32><<<grid, kBatchThreads, 0, s>>>(bd, a);
-        else k_batch_traverse<3, false, 16><<<grid, kBatchThreads, 0, s>>>(bd, a);
+        if (fp32 && b->tpw == 32) launch_batch_traverse<3, true, 32>(stk, grid, s, bd, a);
+        else if (fp32) launch_batch_traverse<3, true, 16>(stk, grid, s, bd, a);
+        else if (b->tpw == 32) launch_batch_traverse<3, false, 32>(stk, grid, s, bd, a);
+        else launch_batch_traverse<3, false, 16>(stk, grid, s, bd, a);
     } else {
-        if (fp32) k_batch_traverse<2, true, 32><<<grid, kBatchThreads, 0, s>>>(bd, a);
-        else k_batch_traverse<2, false, 32><<<grid, kBatchThreads, 0, s>>>(bd, a);
+        if (fp32) launch_batch_traverse<2, true, 32>(stk, grid, s, bd, a);
+        else launch_batch_traverse<2, false, 32>(stk, grid, s, bd, a);
     }
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
@@ -859,6 +939,18 @@ int bhut_batch_set_multipole(bhut_batch* b, int multipole)
     }
     if (multipole != b->multipole) drop_graph(b);
     b->multipole = multipole;
+    return kOk;
+}
+
+int bhut_batch_set_stack(bhut_batch* b, int placement)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (placement != BHUT_STACK_SHARED && placement != BHUT_STACK_REGISTERS) {
+        set_error("unknown stack placement %d", placement);
+        return kInvalid;
+    }
+    if (placement != b->stack) drop_graph(b);
+    b->stack = placement;
     return kOk;
 }
 

@@ -115,7 +115,7 @@ def batched_report(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: i
     _log(f"autotune {cfg} {times}")
     sv = batch.BatchedSolver(leaf_size=cfg["leaf_size"], form="fp32", criterion=criterion,
                              targets_per_warp=cfg["targets_per_warp"], use_graph=True,
-                             multipole=multipole)
+                             multipole=multipole, stack=cfg["stack"])
     sv.load(pd, md, off)
     out = torch.empty_like(pd)
     sv.solve(theta=theta, softening=eps, G=G, out=out)
@@ -161,7 +161,7 @@ def batched_report(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: i
         f"[{nmin}, {nmax}], a ~ U[0.5, 2], own seeds", "particles": ntot, "theta": theta,
         "softening": eps, "form": "fp32", "criterion": criterion, "multipole": multipole,
         "config": cfg,
-        "autotune_s": {f"L{k[0]}_tpw{k[1]}": v for k, v in times.items()},
+        "autotune_s": {f"L{k[0]}_tpw{k[1]}_{k[2]}": v for k, v in times.items()},
         "solve_ms": t_batch * 1e3, "systems_per_s": nsys / t_batch,
         "accels_per_s": ntot / t_batch, "interactions": {"p2p": p2p, "m2p": m2p},
         "plain_per_system": {"systems_timed": int(len(pick)), "systems_per_s": plain_sps,

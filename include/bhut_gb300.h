@@ -171,6 +171,13 @@ BHUT_API int bhut_batch_create(int dim, int leaf_size, void *stream, bhut_batch 
 BHUT_API int bhut_batch_configure(bhut_batch *b, int form, int criterion, int targets_per_warp,
                                   int use_graph);
 
+/* Placement of the batched traversal's per-warp stack (bhut_batch_set_stack):
+ * shared memory, or registers spread over the warp's lanes (two entries per
+ * lane, popped with shuffles).  A tuning choice; results are identical. */
+#define BHUT_STACK_SHARED 0
+#define BHUT_STACK_REGISTERS 1
+BHUT_API int bhut_batch_set_stack(bhut_batch *b, int placement);
+
 /* Node expansion of the batched FP32 form (BHUT_MULTIPOLE_*; default
  * monopole); no counterpart in the reference. */
 BHUT_API int bhut_batch_set_multipole(bhut_batch *b, int multipole);

@@ -93,3 +93,18 @@ def test_batch_2d_and_errors():
         batch.BatchedSolver(form="exact")
     with pytest.raises(ValueError):
         batch.BatchedSolver(form="fast", criterion="bh_offset")
+
+
+@pytest.mark.parametrize("form,tpw", [("fast", 32), ("fp32", 32), ("fp32", 16), ("fast", 16)])
+def test_stack_placements_agree(systems, form, tpw):
+    pos, m, off = batch.concat_systems(systems)
+    res = {}
+    for stk in ("shared", "registers"):
+        sv = batch.BatchedSolver(form=form, targets_per_warp=tpw, use_graph=True, stack=stk)
+        sv.load(pos, m, off)
+        res[stk] = (sv.solve(theta=0.5, softening=0.01), sv.stats())
+        sv.close()
+    assert np.array_equal(res["shared"][0], res["registers"][0])
+    assert res["shared"][1] == res["registers"][1]
+    with pytest.raises(ValueError, match="stack must be"):
+        batch.BatchedSolver(stack="global")
