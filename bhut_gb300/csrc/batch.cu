@@ -460,12 +460,17 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                     const int cn = min(kWarp, c - bb);
                     if (act) {
                         if (sub == 0) cnt[0] += cn - (i >= s0 + bb && i < s0 + bb + cn);
-                        for (int q = sub; q < cn; q += LPT) {
-                            if (FP32) {
+                        if (FP32) {
+                            for (int q = sub; q < cn; q += LPT)
                                 pair_f32<DIM>(Th, Tl, sh[w][q], sl[w][q], e2h, ah, al);
-                            } else if (!pair_ff<DIM, false>(Th, Tl, sh[w][q], sl[w][q], e2h, e2l,
-                                                            ah, al)) {
-                                const int gi = s0 + bb + q;
+                        } else {
+                            unsigned fb = 0;   // pairs left to FP64, taken after the loop
+                            for (int q = sub; q < cn; q += LPT)
+                                fb |= (unsigned)!pair_ff<DIM, false>(Th, Tl, sh[w][q], sl[w][q],
+                                                                     e2h, e2l, ah, al) << q;
+                            while (fb) {
+                                const int gi = s0 + bb + __ffs(fb) - 1;
+                                fb &= fb - 1;
                                 pair_fp64<DIM>(x, y, z, t.sx[gi], t.sy[gi],
                                                DIM == 3 ? t.sz[gi] : 0.0, t.sm[gi], eps2, a64);
                                 cnt[4]++;

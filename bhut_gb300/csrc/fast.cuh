@@ -90,7 +90,9 @@ static __device__ __forceinline__ float comp(const float4& v, int k)
 }
 
 // Adds G-less m * (x_src - x_tgt) / (|dx|^2 + eps^2)^(3/2), normalised
-// units, to (ah, al).  Returns false when the pair must go to FP64.
+// units, to (ah, al).  Returns false when the pair must go to FP64; it then
+// adds exactly zero (the term is computed on a stand-in R and discarded with
+// selects, so the pair loop has no branch).
 //
 // d = hi_src - hi_tgt is exact on the grid and l = lo_src - lo_tgt is small
 // (|l| <= 2^-23), so (d, l) is renormalised with FastTwoSum into (gh, gl),
@@ -130,13 +132,11 @@ __device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4
         lo = __fadd_rn(lo, __fadd_rn(two_sum_err(s, e2h, t), __fmaf_rn(2.0f, c, e2l)));
         s = t;
     }
-    const float Rh = __fadd_rn(s, lo);
-    const float Rl = __fsub_rn(lo, __fsub_rn(Rh, s));
-    if (FAR) {
-        if (!(Rh >= kTinyR && Rh <= kHugeR)) return false;
-    } else {
-        if (!(Rh >= kTinyR)) return false;           // |dx| <= 2 inside the box
-    }
+    const float Rs = __fadd_rn(s, lo);
+    // |dx| <= 2 inside the box: only FAR targets can exceed kHugeR
+    const bool ok = FAR ? (Rs >= kTinyR && Rs <= kHugeR) : (Rs >= kTinyR);
+    const float Rh = ok ? Rs : 1.0f;
+    const float Rl = ok ? __fsub_rn(lo, __fsub_rn(Rs, s)) : 0.0f;
     // w = R^(-3/2): y ~ R^(-1/2); e = 1 - R y^2 exactly enough;
     // w = y^3 (1 - e)^(-3/2) = y^3 (1 + 3e/2 + 15e^2/8 + O(e^3))
     const float y = rsqrt_mufu(Rh);                  // Rh >= kTinyR: normal
@@ -148,9 +148,10 @@ __device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4
     const float corr = __fmul_rn(e, __fmaf_rn(1.875f, e, 1.5f));
     const float wh = W;
     const float wl = __fmaf_rn(W, corr, We);
-    // f = m w
-    const float fh = __fmul_rn(sh.w, wh);
-    const float fl = __fmaf_rn(sh.w, wl, __fmaf_rn(sl.w, wh, __fmaf_rn(sh.w, wh, -fh)));
+    // f = m w (zero for a pair left to FP64)
+    const float mh = ok ? sh.w : 0.0f, ml = ok ? sl.w : 0.0f;
+    const float fh = __fmul_rn(mh, wh);
+    const float fl = __fmaf_rn(mh, wl, __fmaf_rn(ml, wh, __fmaf_rn(mh, wh, -fh)));
 #pragma unroll
     for (int k = 0; k < DIM; k++) {
         const float Fh = __fmul_rn(fh, gh[k]);
@@ -160,7 +161,7 @@ __device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4
         ah[k] = t;
         al[k] = __fadd_rn(al[k], __fadd_rn(err, Fl));
     }
-    return true;
+    return ok;
 }
 
 // FP64 pair in physical units, G-less (the Numba loop arithmetic).
@@ -213,12 +214,12 @@ __device__ __forceinline__ void pair_f32(const float* Th, const float* Tl, float
     const float d2 = DIM == 3 ? __fadd_rn(__fsub_rn(sh.z, Th[2]), __fsub_rn(sl.z, Tl[2])) : 0.0f;
     float r2 = fmaf(d1, d1, fmaf(d0, d0, e2));
     if (DIM == 3) r2 = fmaf(d2, d2, r2);
-    // r^2 + eps^2 == 0: no term (kernels.py:62-63); below the normal range
-    // (closer than 2^-63 box sizes, unsoftened) the FP32 force would overflow:
-    // no term either
-    if (!(r2 >= 0x1p-126f)) return;
-    const float ri = rsqrt_mufu(r2);
-    const float f = sh.w * (ri * ri * ri);
+    // r^2 + eps^2 == 0: no force (kernels.py:62-63); below the normal range
+    // (closer than 2^-63 box sizes, unsoftened) the FP32 force would
+    // overflow: none either.  Selected, not branched: f = 0 then.
+    const bool ok = r2 >= 0x1p-126f;
+    const float ri = rsqrt_mufu(ok ? r2 : 1.0f);
+    const float f = ok ? sh.w * (ri * ri * ri) : 0.0f;
     const float d[3] = {d0, d1, d2};
 #pragma unroll
     for (int k = 0; k < DIM; k++) {            // Kahan compensated sum

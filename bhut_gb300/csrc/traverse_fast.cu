@@ -189,14 +189,17 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                     // is not skipped; it is only left out of the pair count
                     // (bh.py:254).
                     cnt[0] += cn - (me_sorted >= s + b && me_sorted < s + b + cn);
+                    unsigned fb = 0;   // pairs left to FP64 (rare), taken after the loop
 #pragma unroll 2
-                    for (int q = 0; q < cn; q++) {
-                        if (!pair_ff<DIM, FAR>(Th, Tl, sh[w][q], sl[w][q], a.e2h, a.e2l, ah, al)) {
-                            const int gi = s + b + q;
-                            pair_fp64<DIM>(x, y, z, t.sx[gi], t.sy[gi], DIM == 3 ? t.sz[gi] : 0.0,
-                                           t.sm[gi], eps2, a64);
-                            cnt[4]++;
-                        }
+                    for (int q = 0; q < cn; q++)
+                        fb |= (unsigned)!pair_ff<DIM, FAR>(Th, Tl, sh[w][q], sl[w][q], a.e2h,
+                                                           a.e2l, ah, al) << q;
+                    while (fb) {
+                        const int gi = s + b + __ffs(fb) - 1;
+                        fb &= fb - 1;
+                        pair_fp64<DIM>(x, y, z, t.sx[gi], t.sy[gi], DIM == 3 ? t.sz[gi] : 0.0,
+                                       t.sm[gi], eps2, a64);
+                        cnt[4]++;
                     }
                 }
                 __syncwarp();
