@@ -35,7 +35,22 @@ namespace bhut {
 
 constexpr int kFastWarps = 4;
 constexpr int kFastThreads = kFastWarps * kWarp;
-constexpr int kFastBlocksPerSM = 6;    // 24 warps per SM: registers capped at 80
+// Tuning (overridable at build time): resident blocks per SM for the fast
+// form (6: 24 warps per SM, registers capped at 80) and the unroll factors
+// of the leaf pair loops.  Swept on GB300 at 1M Plummer: unroll 4 / 8 beat
+// 1-2 / 1-4 by 2-10 %; 5 blocks per SM (96 registers) gains nothing.
+#ifndef BHUT_FAST_BLOCKS
+#define BHUT_FAST_BLOCKS 6
+#endif
+#ifndef BHUT_FF_UNROLL
+#define BHUT_FF_UNROLL 4
+#endif
+#ifndef BHUT_F32_UNROLL
+#define BHUT_F32_UNROLL 8
+#endif
+constexpr int kFastBlocksPerSM = BHUT_FAST_BLOCKS;
+constexpr int kFFUnroll = BHUT_FF_UNROLL;
+constexpr int kF32Unroll = BHUT_F32_UNROLL;
 
 // ---------------------------------------------------------------------------
 // frame (normalisation) derived from the tree's bounding box
@@ -190,7 +205,7 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                     // (bh.py:254).
                     cnt[0] += cn - (me_sorted >= s + b && me_sorted < s + b + cn);
                     unsigned fb = 0;   // pairs left to FP64 (rare), taken after the loop
-#pragma unroll 2
+#pragma unroll (kFFUnroll)
                     for (int q = 0; q < cn; q++)
                         fb |= (unsigned)!pair_ff<DIM, FAR>(Th, Tl, sh[w][q], sl[w][q], a.e2h,
                                                            a.e2l, ah, al) << q;
@@ -365,7 +380,7 @@ __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, c
                 const int cn = min(kWarp, c - b);
                 if (act) {
                     cnt[0] += cn - (me_sorted >= s + b && me_sorted < s + b + cn);
-#pragma unroll 4
+#pragma unroll (kF32Unroll)
                     for (int q = 0; q < cn; q++)
                         pair_f32<DIM>(T, Tl, sh[w][q], sl[w][q], a.e2h, acc, cmp);
                 }

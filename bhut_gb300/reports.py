@@ -177,7 +177,8 @@ def batched_report(nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: i
 def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: int = 21,
                   plain_seconds: float = 90.0, err_requests: int = 6, theta: float = 0.7,
                   criterion: str = "bh_offset", multipole: str = "quad",
-                  plain_theta: float = 0.5, closed_loop: bool = True, emit: bool = True):
+                  plain_theta: float = 0.5, closed_loop: bool = True, emit: bool = True,
+                  plain_theta_equal_error: float | None = None):
     """``served``: a Poisson stream (mean ``rate`` requests/s) of ``count``
     systems (N log-uniform in [1e3, 2e6], half Plummer, half uniform cubes of
     side 2, velocities N(0, 0.1^2)), each advanced ``steps`` KDK steps
@@ -189,12 +190,14 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
     ``closed_loop`` the server also runs the stream saturated (every request
     queued at t = 0).  Median errors vs FP64 direct sum on the initial
     conditions of requests spread over the size range, for both
-    configurations."""
+    configurations.  ``plain_theta_equal_error`` adds a second plain run at
+    a smaller theta whose error is close to the server's (equal-error
+    comparison)."""
     from . import serve
     reqs = serve.request_stream(count, rate=rate, steps=steps, seed=seed)
     total_n = sum(r.n for r in reqs)
     _log(f"{count} requests, {total_n:,} particles")
-    errs_srv, errs_plain = [], []
+    errs_srv, errs_plain, errs_eq = [], [], []
     by_size = sorted(reqs, key=lambda r: r.n)
     pick = [by_size[int(round(k))] for k in np.linspace(0, len(by_size) - 1, err_requests)]
     for r in pick:
@@ -207,6 +210,10 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
                                 form="fast")
         errs_srv.append(precision.error_distribution(a_s[idx], ref)["median"])
         errs_plain.append(precision.error_distribution(a_p[idx], ref)["median"])
+        if plain_theta_equal_error is not None:
+            a_q = api.accelerations(r.positions, r.masses, theta=plain_theta_equal_error,
+                                    softening=0.01, form="fast")
+            errs_eq.append(precision.error_distribution(a_q[idx], ref)["median"])
     _log(f"median errors: served {errs_srv}, plain {errs_plain}")
     sv = serve.Server(theta=theta, softening=0.01, dt=1e-3, rebuild_every=10, form="fp32",
                       criterion=criterion, multipole=multipole)
@@ -225,6 +232,17 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
     pl = serve.plain_path(reqs2, theta=plain_theta, softening=0.01, dt=1e-3, rebuild_every=10,
                           realtime=True, max_seconds=plain_seconds)
     _log(f"plain: {pl}")
+    equal = None
+    if plain_theta_equal_error is not None:
+        th2 = plain_theta_equal_error
+        e2 = errs_eq
+        pl2 = serve.plain_path(serve.request_stream(count, rate=rate, steps=steps, seed=seed),
+                               theta=th2, softening=0.01, dt=1e-3, rebuild_every=10,
+                               realtime=True, max_seconds=plain_seconds)
+        equal = {"theta": th2, "plain": pl2, "median_err_vs_direct": float(np.median(e2)),
+                 "solves_per_s_ratio": st["solves_per_s"] / pl2["solves_per_s"]
+                 if pl2["solves_per_s"] else None}
+        _log(f"plain at theta={th2}: {equal}")
     line = {"report": "served", "requests": count, "rate_per_s": rate, "steps": steps,
             "particles": total_n,
             "served_config": {"form": "fp32", "theta": theta, "criterion": criterion,
@@ -232,6 +250,7 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
             "plain_config": {"form": "fast", "theta": plain_theta, "criterion": "bh",
                              "multipole": "mono", "leaf_size": 32},
             "served": st, "served_closed_loop": closed, "plain": pl,
+            "plain_equal_error": equal,
             "solves_per_s_ratio": st["solves_per_s"] / pl["solves_per_s"]
             if pl["solves_per_s"] else None,
             "err_requests_n": [r.n for r in pick],
@@ -255,6 +274,7 @@ def main():
     ap.add_argument("--multipole", default=None)
     ap.add_argument("--theta", type=float, default=None)
     ap.add_argument("--thetas", default="0.3,0.5,0.7")
+    ap.add_argument("--plain-theta-equal", type=float, default=None)
     args = ap.parse_args()
     if args.report == "precision":
         precision_report(args.n, args.sample, criterion=args.criterion or "bh",
@@ -267,7 +287,8 @@ def main():
     elif args.report == "served":
         served_report(args.count, criterion=args.criterion or "bh_offset",
                       multipole=args.multipole or "quad",
-                      theta=args.theta if args.theta is not None else 0.7)
+                      theta=args.theta if args.theta is not None else 0.7,
+                      plain_theta_equal_error=args.plain_theta_equal)
 
 
 if __name__ == "__main__":
