@@ -460,9 +460,12 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                     const int cn = min(kWarp, c - bb);
                     if (act) {
                         if (sub == 0) cnt[0] += cn - (i >= s0 + bb && i < s0 + bb + cn);
-                        if (FP32) {
+                        if (FP32) {   // <= 32 terms in FP32, then one Kahan step
+                            float part[3] = {0.f, 0.f, 0.f};
+#pragma unroll 8
                             for (int q = sub; q < cn; q += LPT)
-                                pair_f32<DIM>(Th, Tl, sh[w][q], sl[w][q], e2h, ah, al);
+                                pair_f32_partial<DIM>(Th, Tl, sh[w][q], sl[w][q], e2h, part);
+                            kahan_add_f32<DIM>(part, ah, al);
                         } else {
                             unsigned fb = 0;   // pairs left to FP64, taken after the loop
                             for (int q = sub; q < cn; q += LPT)

@@ -231,6 +231,39 @@ __device__ __forceinline__ void pair_f32(const float* Th, const float* Tl, float
 }
 
 
+// FP32 pair term added to a plain FP32 partial sum p (no compensation): the
+// leaf loop sums at most 32 such terms and then adds the partial to the
+// Kahan-compensated per-target accumulator with kahan_add_f32 (blocked
+// Kahan summation).  Same displacement, r^2 and force as pair_f32.
+template <int DIM>
+__device__ __forceinline__ void pair_f32_partial(const float* Th, const float* Tl, float4 sh,
+                                                 float4 sl, float e2, float* p)
+{
+    const float d0 = __fadd_rn(__fsub_rn(sh.x, Th[0]), __fsub_rn(sl.x, Tl[0]));
+    const float d1 = __fadd_rn(__fsub_rn(sh.y, Th[1]), __fsub_rn(sl.y, Tl[1]));
+    const float d2 = DIM == 3 ? __fadd_rn(__fsub_rn(sh.z, Th[2]), __fsub_rn(sl.z, Tl[2])) : 0.0f;
+    float r2 = fmaf(d1, d1, fmaf(d0, d0, e2));
+    if (DIM == 3) r2 = fmaf(d2, d2, r2);
+    const bool ok = r2 >= 0x1p-126f;
+    const float ri = rsqrt_mufu(ok ? r2 : 1.0f);
+    const float f = ok ? sh.w * (ri * ri * ri) : 0.0f;
+    p[0] = fmaf(f, d0, p[0]);
+    p[1] = fmaf(f, d1, p[1]);
+    if (DIM == 3) p[2] = fmaf(f, d2, p[2]);
+}
+
+template <int DIM>
+__device__ __forceinline__ void kahan_add_f32(const float* p, float* acc, float* cmp)
+{
+#pragma unroll
+    for (int k = 0; k < DIM; k++) {
+        const float y = __fsub_rn(p[k], cmp[k]);
+        const float t = __fadd_rn(acc[k], y);
+        cmp[k] = __fsub_rn(__fsub_rn(t, acc[k]), y);
+        acc[k] = t;
+    }
+}
+
 // A node's monopole plus its Plummer-softened traceless quadrupole (FP32
 // form, multipole "quad"), Kahan-added.  With d = com - x (target to node),
 // r^2 = |d|^2 + eps^2:

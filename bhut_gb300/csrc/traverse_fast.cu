@@ -342,9 +342,11 @@ k_traverse_fast(TreeDev t, FastTree ft, FastArgs a)
 
 // ---------------------------------------------------------------------------
 // form "fp32": the precision form.  Pair terms, monopoles and the opening
-// test in FP32 on the grid-aligned hi coordinates; per-target sums with
-// Kahan compensation.  FP64 stays in the tree build (bounding box, Morton
-// keys, masses and centres of mass) and in the final scaling.
+// test in FP32 on hi + lo displacements (each difference exact, rounded
+// once); per-target sums Kahan-compensated: every monopole, and every leaf
+// block of at most 32 pair terms (summed in FP32 first), is one Kahan step.
+// FP64 stays in the tree build (bounding box, Morton keys, masses and
+// centres of mass, quadrupoles) and in the final scaling.
 // ---------------------------------------------------------------------------
 template <int DIM>
 __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, const FastArgs& a,
@@ -380,9 +382,11 @@ __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, c
                 const int cn = min(kWarp, c - b);
                 if (act) {
                     cnt[0] += cn - (me_sorted >= s + b && me_sorted < s + b + cn);
+                    float part[3] = {0.f, 0.f, 0.f};   // <= 32 terms, then one Kahan step
 #pragma unroll (kF32Unroll)
                     for (int q = 0; q < cn; q++)
-                        pair_f32<DIM>(T, Tl, sh[w][q], sl[w][q], a.e2h, acc, cmp);
+                        pair_f32_partial<DIM>(T, Tl, sh[w][q], sl[w][q], a.e2h, part);
+                    kahan_add_f32<DIM>(part, acc, cmp);
                 }
                 __syncwarp();
             }
