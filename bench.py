@@ -227,10 +227,12 @@ def measure_gemm_peak(torch, dtype) -> float:
 # rsqrt and cube 11, m * w 4, three float-float products and accumulations
 # 36 -> 107 (plus one MUFU rsqrt).
 FF_OPS_PER_INTERACTION = 107
-# ... and of one FP32/Kahan pair term of the fp32 form (pair_f32, fast.cuh):
-# displacement 9, r^2 + eps^2 3, check 1, cube 2, m * w 1, three Kahan
-# products and additions 15 -> 31 (plus one MUFU rsqrt).
-F32_OPS_PER_INTERACTION = 31
+# ... and of the fp32 form (fast.cuh): a pair term (pair_f32_partial:
+# displacement 9, r^2 + eps^2 3, cube 2, m * w 1, three FMAs into the leaf
+# partial 3 -> 18) and a monopole (pair_f32: the same 15 plus a Kahan step
+# per component 12 -> 27), each plus one MUFU rsqrt.
+F32_OPS_PER_PAIR = 18
+F32_OPS_PER_MONOPOLE = 27
 
 
 def run_ours(args, ws, rank, local):
@@ -322,8 +324,13 @@ def run_ours(args, ws, rank, local):
             "work_rule": f"{FLOPS_PER_INTERACTION} flop x (pair + monopole evaluations counted "
                          "by the kernel)"}
     else:
-        per = FF_OPS_PER_INTERACTION if args.form == "fast" else F32_OPS_PER_INTERACTION
-        ops = per * inter
+        if args.form == "fast":
+            ops = FF_OPS_PER_INTERACTION * inter
+            rule = f"{FF_OPS_PER_INTERACTION} FP32 ops per float-float pair or monopole term"
+        else:
+            ops = F32_OPS_PER_PAIR * p2p + F32_OPS_PER_MONOPOLE * m2p
+            rule = (f"{F32_OPS_PER_PAIR} FP32 ops per pair term, {F32_OPS_PER_MONOPOLE} per "
+                    "Kahan-added monopole")
         achieved32 = ops / trav_s / 1e12
         fma_rate = peak32 / 2.0      # FP32 pipe lane-instructions per second (one FMA = 2 flop)
         roofline = {
@@ -335,8 +342,7 @@ def run_ours(args, ws, rank, local):
             "peak_source": "cuBLAS SGEMM 4096^3 (TF32 off) measured in this run, / 2 for the "
                            "FMA-instruction rate (MEASURED_PEAKS.json has no FP32 figure)",
             "work_per_launch": ops,
-            "work_rule": f"{per} FP32 ops per pair/monopole term of form {args.form} "
-                         "x evaluations counted by the kernel",
+            "work_rule": f"{rule} x evaluations counted by the kernel",
             "fp64_equivalent": {"achieved": achieved64, "peak": peak64, "unit": "TFLOP/s",
                                 "frac": achieved64 / peak64,
                                 "rule": f"{FLOPS_PER_INTERACTION} flop per interaction vs "

@@ -237,7 +237,7 @@ k_seg_frames(TreeDev t, const int64_t* __restrict__ part_off, const int64_t* __r
              FastFrame* __restrict__ frames, float4* __restrict__ ph, float4* __restrict__ pl,
              float4* __restrict__ nh, float4* __restrict__ nl, float* __restrict__ nsize,
              float* __restrict__ ndelta, const double* __restrict__ quad, float4* __restrict__ nq0,
-             float2* __restrict__ nq1)
+             float2* __restrict__ nq1, int4* __restrict__ nhdr)
 {
     const int s = blockIdx.x;
     const int dim = t.dim;
@@ -259,6 +259,7 @@ k_seg_frames(TreeDev t, const int64_t* __restrict__ part_off, const int64_t* __r
     }
     for (int64_t k = node_off[s] + threadIdx.x; k < node_off[s + 1]; k += blockDim.x) {
         const NodeCM c = t.cm[k];
+        nhdr[k] = make_int4(t.first_child[k], t.start[k], t.count[k], c.w != 0.0);
         float4 h, l;
         split_grid(__dmul_rn(__dsub_rn(c.x, f.c[0]), f.s), h.x, l.x);
         split_grid(__dmul_rn(__dsub_rn(c.y, f.c[1]), f.s), h.y, l.y);
@@ -301,6 +302,7 @@ struct BatchDev {
     const float* ndelta;
     const float4* nq0;            // quadrupoles (FP32 form); NULL: monopoles
     const float2* nq1;
+    const int4* nhdr;             // (first_child, start, count, mass != 0)
 };
 
 struct BatchArgs {
@@ -446,10 +448,11 @@ k_batch_traverse(BatchDev b, BatchArgs a)
             const int node = e.x;
             const bool act = ((unsigned)e.y >> lane) & 1u;
             cnt[2] += act && sub == 0;
-            if (mass_is_zero(t.cm + node)) continue;
-            const int fc = t.first_child[node];
+            const int4 hd = b.nhdr[node];   // (first_child, start, count, mass != 0)
+            if (!hd.w) continue;
+            const int fc = hd.x;
             if (fc < 0) {
-                const int s0 = t.start[node], c = t.count[node];
+                const int s0 = hd.y, c = hd.z;
                 for (int bb = 0; bb < c; bb += kWarp) {
                     const int jj = bb + lane;
                     if (jj < c) {
@@ -626,7 +629,7 @@ struct bhut_batch {
     BufB pos, mass, d_part_off, d_node_off, d_leaf_off, d_tasks, keys, perm, sys_of, key2,
         sx, sy, sz, sm, cm, size, center, half, lo, hi, first_child, start, count, parent,
         leaf_list, arrive, sort_scratch, box, frames, ph, pl, nh, nl, nsize, ndelta, counter,
-        err, stats, out, keep, perm_in, quad, nq0, nq1;
+        err, stats, out, keep, perm_in, quad, nq0, nq1, nhdr;
     bool keep_active = false;
     unsigned long long last_stats[5] = {0, 0, 0, 0, 0};
     cudaGraphExec_t graph = nullptr;
@@ -638,7 +641,7 @@ struct bhut_batch {
                      &sys_of, &key2, &sx, &sy, &sz, &sm, &cm, &size, &center, &half, &lo, &hi,
                      &first_child, &start, &count, &parent, &leaf_list, &arrive, &sort_scratch,
                      &box, &frames, &ph, &pl, &nh, &nl, &nsize, &ndelta, &counter, &err, &stats,
-                     &out, &keep, &perm_in, &quad, &nq0, &nq1, nullptr};
+                     &out, &keep, &perm_in, &quad, &nq0, &nq1, &nhdr, nullptr};
 
     TreeDev dev() const
     {
@@ -744,6 +747,7 @@ int plan_layout(bhut_batch* b, const int64_t* offsets, int64_t nsys)
     BHUT_TRY(b->quad.ensure(sizeof(double) * 6 * mtot, s));
     BHUT_TRY(b->nq0.ensure(sizeof(float4) * mtot, s));
     BHUT_TRY(b->nq1.ensure(sizeof(float2) * mtot, s));
+    BHUT_TRY(b->nhdr.ensure(sizeof(int4) * mtot, s));
     BHUT_TRY(b->box.ensure(sizeof(double) * 8 * nsys, s));
     BHUT_TRY(b->frames.ensure(sizeof(FastFrame) * nsys, s));
     BHUT_TRY(b->sort_scratch.ensure(sort_scratch_bytes(b->ntot), s));
@@ -823,7 +827,8 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
         b->dev(), b->d_part_off.as<int64_t>(), b->d_node_off.as<int64_t>(), b->box.as<double>(),
         b->center.as<double>(), b->frames.as<FastFrame>(), b->ph.as<float4>(), b->pl.as<float4>(),
         b->nh.as<float4>(), b->nl.as<float4>(), b->nsize.as<float>(), b->ndelta.as<float>(),
-        quad ? b->quad.as<double>() : nullptr, b->nq0.as<float4>(), b->nq1.as<float2>());
+        quad ? b->quad.as<double>() : nullptr, b->nq0.as<float4>(), b->nq1.as<float2>(),
+        b->nhdr.as<int4>());
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
     // traversal
@@ -833,7 +838,7 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
                 b->frames.as<FastFrame>(), b->ph.as<float4>(), b->pl.as<float4>(),
                 b->nh.as<float4>(), b->nl.as<float4>(), b->nsize.as<float>(),
                 b->ndelta.as<float>(), quad ? b->nq0.as<float4>() : nullptr,
-                quad ? b->nq1.as<float2>() : nullptr};
+                quad ? b->nq1.as<float2>() : nullptr, b->nhdr.as<int4>()};
     BatchArgs a{b->d_tasks.as<int2>(), (int)b->tasks.size(), b->counter.as<unsigned>(), theta,
                 eps, G, b->mac, out, b->err.as<unsigned>(), b->stats.as<unsigned long long>()};
     const unsigned grid = 152u * 6u;   // persistent: about one wave of resident blocks

@@ -112,7 +112,7 @@ struct bhut_tree {
     // traversal targets
     DevBuf tpos, tkeys, tperm, tx, ty, tz, tbox, out;
     // float-float copies for the fast form
-    DevBuf frame, ph, pl, nh, nl, nsize, ndelta, th, tl, quad, nq0, nq1;
+    DevBuf frame, ph, pl, nh, nl, nsize, ndelta, th, tl, quad, nq0, nq1, nhdr;
     bool ff_valid = false;
     bool ff_quad = false;
     int mac = 0;
@@ -290,6 +290,7 @@ int prepare_fast(bhut_tree* t)
     BHUT_TRY(t->nl.ensure(sizeof(float4) * t->m, s));
     BHUT_TRY(t->nsize.ensure(sizeof(float) * t->m, s));
     BHUT_TRY(t->ndelta.ensure(sizeof(float) * t->m, s));
+    BHUT_TRY(t->nhdr.ensure(sizeof(int4) * t->m, s));
     const bool quad = t->multipole == BHUT_MULTIPOLE_QUAD && t->form == BHUT_FORM_FP32;
     if (quad) {
         BHUT_TRY(t->quad.ensure(sizeof(double) * 6 * t->m, s));
@@ -305,7 +306,8 @@ int prepare_fast(bhut_tree* t)
                                  t->center.as<double>(), t->ph.as<float4>(), t->pl.as<float4>(),
                                  t->nh.as<float4>(), t->nl.as<float4>(), t->nsize.as<float>(),
                                  t->ndelta.as<float>(), quad ? t->quad.as<double>() : nullptr,
-                                 t->nq0.as<float4>(), t->nq1.as<float2>(), s));
+                                 t->nq0.as<float4>(), t->nq1.as<float2>(), t->nhdr.as<int4>(),
+                                 s));
     t->ff_quad = quad;
     t->ff_valid = true;
     return kOk;
@@ -316,7 +318,7 @@ FastTree fast_tree(const bhut_tree* t)
     return FastTree{t->frame.as<FastFrame>(), t->ph.as<float4>(), t->pl.as<float4>(),
                     t->nh.as<float4>(), t->nl.as<float4>(), t->nsize.as<float>(),
                     t->ndelta.as<float>(), t->ff_quad ? t->nq0.as<float4>() : nullptr,
-                    t->ff_quad ? t->nq1.as<float2>() : nullptr};
+                    t->ff_quad ? t->nq1.as<float2>() : nullptr, t->nhdr.as<int4>()};
 }
 
 // Scale of the fast form's normalised coordinates (the frame's s), read
@@ -634,7 +636,7 @@ void bhut_tree_destroy(bhut_tree* t)
                      &t->sort_scratch, &t->box_partial, &t->box, &t->counters, &t->err, &t->stats,
                      &t->tpos, &t->tkeys, &t->tperm, &t->tx, &t->ty, &t->tz, &t->tbox, &t->out,
                      &t->frame, &t->ph, &t->pl, &t->nh, &t->nl, &t->nsize, &t->ndelta, &t->th,
-                     &t->tl, &t->quad, &t->nq0, &t->nq1};
+                     &t->tl, &t->quad, &t->nq0, &t->nq1, &t->nhdr};
     for (DevBuf* b : all) b->release(s);
     cudaStreamSynchronize(s);
     if (t->own_stream) cudaStreamDestroy(s);

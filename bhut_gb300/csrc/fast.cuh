@@ -68,13 +68,6 @@ static __device__ __forceinline__ float two_sum_err(float a, float b, float s)
     return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// mass == +-0 of a node, with 32-bit integer operations on the two words.
-static __device__ __forceinline__ bool mass_is_zero(const NodeCM* c)
-{
-    const int2 w = __ldg(reinterpret_cast<const int2*>(&c->w));
-    return ((w.y & 0x7fffffff) | w.x) == 0;
-}
-
 // MUFU reciprocal square root, flush-to-zero (one instruction; callers pass
 // normal, positive arguments only).
 static __device__ __forceinline__ float rsqrt_mufu(float x)

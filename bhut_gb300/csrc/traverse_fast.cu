@@ -79,17 +79,19 @@ __global__ void k_ff_particles(const double* __restrict__ sx, const double* __re
     }
 }
 
-__global__ void k_ff_nodes(const NodeCM* __restrict__ cm, const double* __restrict__ size,
-                           const double* __restrict__ center, int64_t m, int dim,
+__global__ void k_ff_nodes(TreeDev t, const double* __restrict__ center,
                            const FastFrame* __restrict__ fr, float4* __restrict__ nh,
                            float4* __restrict__ nl, float* __restrict__ nsize,
                            float* __restrict__ ndelta, const double* __restrict__ quad,
-                           float4* __restrict__ nq0, float2* __restrict__ nq1)
+                           float4* __restrict__ nq0, float2* __restrict__ nq1,
+                           int4* __restrict__ nhdr)
 {
     const FastFrame f = *fr;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m;
+    const int dim = t.dim;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < t.m;
          k += (int64_t)gridDim.x * blockDim.x) {
-        NodeCM c = cm[k];
+        NodeCM c = t.cm[k];
+        nhdr[k] = make_int4(t.first_child[k], t.start[k], t.count[k], c.w != 0.0);
         float4 h, l;
         // a node's COM lies inside the box: |u| <= 1 up to rounding
         split_grid(__dmul_rn(__dsub_rn(c.x, f.c[0]), f.s), h.x, l.x);
@@ -99,7 +101,7 @@ __global__ void k_ff_nodes(const NodeCM* __restrict__ cm, const double* __restri
         split_plain(__dmul_rn(c.w, f.ms), h.w, l.w);
         nh[k] = h;
         nl[k] = l;
-        nsize[k] = __double2float_rn(__dmul_rn(size[k], f.s));
+        nsize[k] = __double2float_rn(__dmul_rn(t.size[k], f.s));
         // distance between the centre of mass and the AABB centre (offset MAC)
         double dd = 0.0;
         for (int d = 0; d < dim; d++) {
@@ -185,11 +187,11 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
         const unsigned mask = (unsigned)e.y;
         const bool act = (mask >> lane) & 1u;
         cnt[2] += act;
-        // mass == 0 skip (bh.py:514), tested on the bits: +-0.0 only
-        if (mass_is_zero(t.cm + node)) continue;
-        const int fc = t.first_child[node];
+        const int4 hd = ft.nhdr[node];   // (first_child, start, count, mass != 0)
+        if (!hd.w) continue;              // mass == 0 skip (bh.py:514)
+        const int fc = hd.x;
         if (fc < 0) {
-            const int s = t.start[node], c = t.count[node];
+            const int s = hd.y, c = hd.z;
             for (int b = 0; b < c; b += kWarp) {
                 const int jj = b + lane;
                 if (jj < c) {
@@ -368,10 +370,11 @@ __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, c
         const unsigned mask = (unsigned)e.y;
         const bool act = (mask >> lane) & 1u;
         cnt[2] += act;
-        if (mass_is_zero(t.cm + node)) continue;
-        const int fc = t.first_child[node];
+        const int4 hd = ft.nhdr[node];   // (first_child, start, count, mass != 0)
+        if (!hd.w) continue;
+        const int fc = hd.x;
         if (fc < 0) {
-            const int s = t.start[node], c = t.count[node];
+            const int s = hd.y, c = hd.z;
             for (int b = 0; b < c; b += kWarp) {
                 const int jj = b + lane;
                 if (jj < c) {
@@ -484,13 +487,13 @@ k_traverse_fp32(TreeDev t, FastTree ft, FastArgs a)
 int launch_fast_prepare(const double* box, int dim, FastFrame* frame, const TreeDev& t,
                         const double* center, float4* ph, float4* pl, float4* nh, float4* nl,
                         float* nsize, float* ndelta, const double* quad, float4* nq0,
-                        float2* nq1, cudaStream_t s)
+                        float2* nq1, int4* nhdr, cudaStream_t s)
 {
     k_frame<<<1, 32, 0, s>>>(box, dim, frame);
     k_ff_particles<<<grid_for(t.n, 256), 256, 0, s>>>(t.sx, t.sy, t.sz, t.sm, t.n, dim, frame, ph,
                                                       pl);
-    k_ff_nodes<<<grid_for(t.m, 256), 256, 0, s>>>(t.cm, t.size, center, t.m, dim, frame, nh, nl,
-                                                  nsize, ndelta, quad, nq0, nq1);
+    k_ff_nodes<<<grid_for(t.m, 256), 256, 0, s>>>(t, center, frame, nh, nl, nsize, ndelta, quad,
+                                                  nq0, nq1, nhdr);
     BHUT_CUDA(cudaGetLastError());
     note_launches(3);
     return kOk;

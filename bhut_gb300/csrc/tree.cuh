@@ -69,6 +69,7 @@ struct FastTree {
     const float* ndelta; // |com - AABB centre|, normalised, per node (offset criterion)
     const float4* nq0;   // quadrupole (xx, yy, zz, xy), normalised, per node; NULL: monopoles
     const float2* nq1;   // quadrupole (xz, yz)
+    const int4* nhdr;    // (first_child, start, count, mass != 0) per node: one load per visit
 };
 
 // Morton encoding (bhut/utils/morton.py:14-45, 183-198) and the quantisation
@@ -156,7 +157,7 @@ int launch_traverse_exact(const TreeDev& t, const double* tx, const double* ty, 
 int launch_fast_prepare(const double* box, int dim, FastFrame* frame, const TreeDev& t,
                         const double* center, float4* ph, float4* pl, float4* nh, float4* nl,
                         float* nsize, float* ndelta, const double* quad, float4* nq0,
-                        float2* nq1, cudaStream_t s);
+                        float2* nq1, int4* nhdr, cudaStream_t s);
 int launch_fast_targets(const double* tx, const double* ty, const double* tz, int64_t nt, int dim,
                         const FastFrame* frame, float4* th, float4* tl, cudaStream_t s);
 int launch_traverse_fast(const TreeDev& t, const FastTree& ft, const float4* th, const float4* tl,
