@@ -193,4 +193,43 @@ def test_plummer_1m_forces(golden_plummer, plummer_1m, oracle_mod, form):
     sub = idx[:2048] % len(tg)
     ref_t = oracle_mod.accelerations(ot, pos, m, theta=0.5, softening=eps, targets=tg[sub])
     assert rel_l2(at[sub], ref_t) <= PLAIN_RTOL
+    # then refit after positions += 0.01 N(0, 1), then rebuild (the rest of the
+    # 1M workload): tree arrays bit-exact, forces within the bar
+    pos2 = pos + 0.01 * np.random.default_rng(21).standard_normal(pos.shape)
+    tree.refit(pos2)
+    assert oracle_mod.should_refit(ot, pos2)
+    ot2 = oracle_mod.refit(ot, pos2, m)
+    td = tree._tree
+    for f in ("mass", "com", "center", "half_size", "first_child", "start", "count", "perm"):
+        assert np.array_equal(np.asarray(getattr(td, f)), np.asarray(getattr(ot2, f))), f
+    acc2 = tree.accelerations(theta=0.5, softening=eps)
+    ref2 = oracle_mod.accelerations(ot2, pos2, m, theta=0.5, softening=eps, self_index=idx[:1024])
+    assert rel_l2(acc2[idx[:1024]], ref2) <= PLAIN_RTOL
+    tree.rebuild(pos2)
+    ot3 = oracle_mod.build_tree(pos2, m, 32)
+    td = tree._tree
+    for f in ("mass", "com", "first_child", "perm"):
+        assert np.array_equal(np.asarray(getattr(td, f)), np.asarray(getattr(ot3, f))), f
+    acc3 = tree.accelerations(theta=0.5, softening=eps)
+    ref3 = oracle_mod.accelerations(ot3, pos2, m, theta=0.5, softening=eps, self_index=idx[:1024])
+    assert rel_l2(acc3[idx[:1024]], ref3) <= PLAIN_RTOL
+    tree.close()
+
+
+@pytest.mark.slow
+def test_plummer_8m_against_oracle(oracle_mod):
+    """Eight million particles: every tree array bit-exact against the
+    oracle's build, forces on 1024 oracle-checked targets within the
+    plain-path bar."""
+    pos, m = workloads.plummer(8_000_000, seed=8)
+    tree = bh.Tree(pos, m, leaf_size=32, form="fast").build()
+    ot = oracle_mod.build_tree(pos, m, 32)
+    td = tree._tree
+    for f in ("perm", "first_child", "count", "mass", "com", "center", "half_size"):
+        assert np.array_equal(np.asarray(getattr(td, f)), np.asarray(getattr(ot, f))), f
+    acc = tree.accelerations(theta=0.5, softening=0.01)
+    idx = np.random.default_rng(3).choice(len(pos), 1024, replace=False)
+    ref = oracle_mod.accelerations(ot, pos, m, theta=0.5, softening=0.01, self_index=idx)
+    assert rel_l2(acc[idx], ref) <= PLAIN_RTOL
+    assert np.all(np.isfinite(acc))
     tree.close()
