@@ -583,14 +583,46 @@ k_batch_traverse(BatchDev b, BatchArgs a)
     }
 }
 
+// Persistent grid: as many blocks as fit on the GPU at once for this
+// variant (its register count decides: 5 to 8 blocks of 128 per SM).
+template <int DIM, bool FP32, int TPW, int STK>
+unsigned persistent_grid()
+{
+    static unsigned grid = 0;
+    if (grid == 0) {
+        int per_sm = 0, dev = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &per_sm, k_batch_traverse<DIM, FP32, TPW, STK>, kBatchThreads, 0) != cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 6;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            sms <= 0)
+            sms = 152;
+        cudaGetLastError();
+        grid = (unsigned)(per_sm * sms);
+    }
+    return grid;
+}
+
+// Runs the occupancy query of the configured variant once, before any
+// stream capture.
 template <int DIM, bool FP32, int TPW>
-void launch_batch_traverse(int stk, unsigned grid, cudaStream_t s, const BatchDev& bd,
-                           const BatchArgs& a)
+void prime_grid_of(int stk)
+{
+    if (stk == BHUT_STACK_REGISTERS) persistent_grid<DIM, FP32, TPW, 1>();
+    else persistent_grid<DIM, FP32, TPW, 0>();
+}
+
+template <int DIM, bool FP32, int TPW>
+void launch_batch_traverse(int stk, cudaStream_t s, const BatchDev& bd, const BatchArgs& a)
 {
     if (stk == BHUT_STACK_REGISTERS)
-        k_batch_traverse<DIM, FP32, TPW, 1><<<grid, kBatchThreads, 0, s>>>(bd, a);
+        k_batch_traverse<DIM, FP32, TPW, 1>
+            <<<persistent_grid<DIM, FP32, TPW, 1>(), kBatchThreads, 0, s>>>(bd, a);
     else
-        k_batch_traverse<DIM, FP32, TPW, 0><<<grid, kBatchThreads, 0, s>>>(bd, a);
+        k_batch_traverse<DIM, FP32, TPW, 0>
+            <<<persistent_grid<DIM, FP32, TPW, 0>(), kBatchThreads, 0, s>>>(bd, a);
 }
 
 inline size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -841,17 +873,16 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
                 quad ? b->nq1.as<float2>() : nullptr, b->nhdr.as<int4>()};
     BatchArgs a{b->d_tasks.as<int2>(), (int)b->tasks.size(), b->counter.as<unsigned>(), theta,
                 eps, G, b->mac, out, b->err.as<unsigned>(), b->stats.as<unsigned long long>()};
-    const unsigned grid = 152u * 6u;   // persistent: about one wave of resident blocks
     const bool fp32 = b->form == BHUT_FORM_FP32;
     const int stk = b->stack;
     if (dim == 3) {
-        if (fp32 && b->tpw == 32) launch_batch_traverse<3, true, 32>(stk, grid, s, bd, a);
-        else if (fp32) launch_batch_traverse<3, true, 16>(stk, grid, s, bd, a);
-        else if (b->tpw == 32) launch_batch_traverse<3, false, 32>(stk, grid, s, bd, a);
-        else launch_batch_traverse<3, false, 16>(stk, grid, s, bd, a);
+        if (fp32 && b->tpw == 32) launch_batch_traverse<3, true, 32>(stk, s, bd, a);
+        else if (fp32) launch_batch_traverse<3, true, 16>(stk, s, bd, a);
+        else if (b->tpw == 32) launch_batch_traverse<3, false, 32>(stk, s, bd, a);
+        else launch_batch_traverse<3, false, 16>(stk, s, bd, a);
     } else {
-        if (fp32) launch_batch_traverse<2, true, 32>(stk, grid, s, bd, a);
-        else launch_batch_traverse<2, false, 32>(stk, grid, s, bd, a);
+        if (fp32) launch_batch_traverse<2, true, 32>(stk, s, bd, a);
+        else launch_batch_traverse<2, false, 32>(stk, s, bd, a);
     }
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
@@ -996,6 +1027,18 @@ int bhut_batch_solve(bhut_batch* b, double theta, double softening, double G, do
     BHUT_TRY(ensure_topology(b));
     const bool dev_out = is_device_pointer(out);
     double* dst = dev_out ? out : b->out.as<double>();
+    {
+        const bool fp32 = b->form == BHUT_FORM_FP32;
+        if (b->dim == 3) {
+            if (fp32 && b->tpw == 32) prime_grid_of<3, true, 32>(b->stack);
+            else if (fp32) prime_grid_of<3, true, 16>(b->stack);
+            else if (b->tpw == 32) prime_grid_of<3, false, 32>(b->stack);
+            else prime_grid_of<3, false, 16>(b->stack);
+        } else {
+            if (fp32) prime_grid_of<2, true, 32>(b->stack);
+            else prime_grid_of<2, false, 32>(b->stack);
+        }
+    }
     if (b->use_graph) {
         if (!b->graph || theta != b->g_theta || softening != b->g_eps || G != b->g_G ||
             dst != b->g_out) {

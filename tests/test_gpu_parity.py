@@ -233,3 +233,20 @@ def test_plummer_8m_against_oracle(oracle_mod):
     assert rel_l2(acc[idx], ref) <= PLAIN_RTOL
     assert np.all(np.isfinite(acc))
     tree.close()
+
+
+def test_plummer_1m_all_targets_fast_vs_exact(plummer_1m):
+    """Full-N coverage at 1M: the float-float form against the FP64 form
+    (itself within 1e-12 of the oracle on samples) on every target, and the
+    same interaction counts."""
+    pos, m = plummer_1m
+    tree = bh.Tree(pos, m, leaf_size=32, form="exact").build()
+    ax = tree.accelerations(theta=0.5, softening=0.01)
+    sx = tree._handle.stats()
+    af = tree.set_form("fast").accelerations(theta=0.5, softening=0.01)
+    sf = tree._handle.stats()
+    tree.close()
+    assert sx[:2] == sf[:2]
+    assert rel_l2(af, ax) <= FAST_RTOL
+    per = np.linalg.norm(af - ax, axis=1) / np.linalg.norm(ax, axis=1)
+    assert np.max(per) < 1e-9, np.max(per)
