@@ -141,6 +141,7 @@ class Server:
         self.active: list[Request] = []
         self.finished: list[Request] = []
         self.ticks = 0
+        self._solve_events = []
         self.solves = 0
         self.accels = 0
         self.peak_bytes = 0.0
@@ -202,7 +203,12 @@ class Server:
         else:
             self.solver.load(self.x, self.m, self.off)
             _lib.check(self.L.bhut_batch_keep_order(self.solver.h, None, None))
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
         self.solver.solve(theta=self.theta, softening=self.eps, G=self.G, out=self.a)
+        ev1.record()
+        self._solve_events.append((ev0, ev1))
         _lib.check(self.L.bhut_batch_order(self.solver.h, self.perm.data_ptr()))
         for k, r in enumerate(self.active):
             s, e = r.slot
@@ -262,6 +268,9 @@ class Server:
                     r.final_velocities = r.velocities.clone()
                 changed = bool(self.active)
         wall = now()
+        torch.cuda.synchronize()
+        solve_s = sum(a.elapsed_time(b) for a, b in self._solve_events) / 1e3
+        self._solve_events = []
         lat = np.array([r.latency for r in self.finished if r.latency is not None])
         return {
             "requests_done": len(self.finished), "wall_s": wall, "ticks": self.ticks,
@@ -270,6 +279,8 @@ class Server:
             "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else None,
             "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None,
             "peak_resident_bytes_est": self.peak_bytes,
+            "solve_device_s": solve_s,
+            "solve_share_of_wall": solve_s / wall if wall else None,
         }
 
     def close(self):
