@@ -669,11 +669,15 @@ struct bhut_batch {
     double g_theta = -1, g_eps = -1, g_G = 0;
     double* g_out = nullptr;
 
-    BufB* all[46] = {&pos, &mass, &d_part_off, &d_node_off, &d_leaf_off, &d_tasks, &keys, &perm,
-                     &sys_of, &key2, &sx, &sy, &sz, &sm, &cm, &size, &center, &half, &lo, &hi,
-                     &first_child, &start, &count, &parent, &leaf_list, &arrive, &sort_scratch,
-                     &box, &frames, &ph, &pl, &nh, &nl, &nsize, &ndelta, &counter, &err, &stats,
-                     &out, &keep, &perm_in, &quad, &nq0, &nq1, &nhdr, nullptr};
+    void release_all()
+    {
+        for (BufB* x : {&pos, &mass, &d_part_off, &d_node_off, &d_leaf_off, &d_tasks, &keys, &perm,
+                        &sys_of, &key2, &sx, &sy, &sz, &sm, &cm, &size, &center, &half, &lo, &hi,
+                        &first_child, &start, &count, &parent, &leaf_list, &arrive,
+                        &sort_scratch, &box, &frames, &ph, &pl, &nh, &nl, &nsize, &ndelta,
+                        &counter, &err, &stats, &out, &keep, &perm_in, &quad, &nq0, &nq1, &nhdr})
+            x->release(stream);
+    }
 
     TreeDev dev() const
     {
@@ -1137,7 +1141,7 @@ void bhut_batch_destroy(bhut_batch* b)
 {
     if (!b) return;
     drop_graph(b);
-    for (BufB* x : b->all) if (x) x->release(b->stream);
+    b->release_all();
     cudaStreamSynchronize(b->stream);
     if (b->own_stream) cudaStreamDestroy(b->stream);
     delete b;

@@ -53,6 +53,38 @@ def sampled_errors(positions, masses, acc, *, softening: float, G: float = 1.0,
     return error_distribution(np.asarray(acc)[idx], ref)
 
 
+def accelerations_with_errors(positions, masses, *, theta: float = 0.5, softening: float = 0.0,
+                              G: float = 1.0, form: str = "fp32", criterion: str = "bh",
+                              multipole: str = "mono", leaf_size: int = 32,
+                              n_sample: int = 1024, seed: int = 0):
+    """Self accelerations together with their relative-error distribution
+    against the FP64 direct sum at ``n_sample`` seeded targets:
+    returns (accelerations, distribution)."""
+    acc = api.accelerations(positions, masses, theta=theta, softening=softening, G=G,
+                            form=form, criterion=criterion, multipole=multipole,
+                            leaf_size=leaf_size)
+    pos = np.asarray(api._host(positions))
+    m = np.asarray(api._host(masses))
+    host = acc.cpu().numpy() if api._is_torch(acc) else np.asarray(acc)
+    dist = sampled_errors(pos, m, host, softening=softening, G=G, n_sample=n_sample, seed=seed)
+    return acc, dist
+
+
+def batched_with_errors(systems, *, theta: float = 0.5, softening: float = 0.0, G: float = 1.0,
+                        form: str = "fp32", criterion: str = "bh", multipole: str = "mono",
+                        leaf_size: int = 32, n_sample: int = 256, seed: int = 0):
+    """Batched solve of [(positions, masses), ...]; every system's result
+    comes with its own error distribution against the FP64 direct sum at up
+    to ``n_sample`` seeded targets: returns [(accelerations, distribution)]."""
+    from . import batch
+    accs = batch.batched_accelerations(systems, theta=theta, softening=softening, G=G,
+                                       leaf_size=leaf_size, form=form, criterion=criterion,
+                                       multipole=multipole)
+    return [(a, sampled_errors(np.asarray(p), np.asarray(m), a, softening=softening, G=G,
+                               n_sample=n_sample, seed=seed))
+            for (p, m), a in zip(systems, accs)]
+
+
 def autotune_leaf_size(positions, masses, *, theta: float, softening: float, G: float = 1.0,
                        form: str = "fp32", criterion: str = "bh", multipole: str = "mono",
                        candidates=(8, 16, 32, 64), repeats: int = 2) -> tuple[int, dict]:

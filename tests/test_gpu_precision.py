@@ -126,3 +126,16 @@ def test_quadrupoles_reduce_error(plummer200k, theta):
     assert np.array_equal(a0, b0)
     with pytest.raises(ValueError, match="multipole must be 'mono'"):
         bh.accelerations(small, sm, form="fast", multipole="quad")
+
+
+def test_results_carry_error_distributions():
+    pos, m = workloads.plummer(20_000, seed=12)
+    acc, dist = precision.accelerations_with_errors(pos, m, theta=0.5, softening=0.01,
+                                                    multipole="quad", n_sample=512)
+    assert acc.shape == pos.shape and dist["n"] == 512
+    assert 0 < dist["median"] < 1e-3 and dist["median"] <= dist["p99"] <= dist["max"]
+    systems = workloads.plummer_batch(4, 300, 3000, seed=2)
+    out = precision.batched_with_errors(systems, theta=0.5, softening=0.01, n_sample=128)
+    assert len(out) == 4
+    for (p, _), (a, d) in zip(systems, out):
+        assert a.shape == p.shape and d["n"] == min(128, len(p)) and d["median"] < 1e-2
