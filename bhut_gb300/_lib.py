@@ -62,6 +62,15 @@ SIGNATURES = {
     "bhut_direct_accelerations": (_INT, [_VP, _VP, _I64, _INT, _VP, _I64, _D, _D, _VP, _VP]),
     "bhut_tree_statistics": (_INT, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _I64, _INT, _VP, _I64, _D,
                                     _VP, _VP]),
+    "bhut_aabb": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),
+    "bhut_normalize_to_unit": (_INT, [_VP, _I64, _INT, _VP, _VP, _D, _VP, _VP]),
+    "bhut_morton_codes_unit": (_INT, [_VP, _I64, _INT, _INT, _VP, _VP]),
+    "bhut_sort_morton_unit": (_INT, [_VP, _I64, _INT, _INT, _VP, _VP, _VP]),
+    "bhut_gather_rows": (_INT, [_VP, _I64, _I64, _VP, _VP, _VP]),
+    "bhut_should_refit": (_INT, [_VP, _I64, _INT, _VP, _D, _VP, _VP]),
+    "bhut_tree_refit_only": (_INT, [_VP, _VP, _VP, _I64]),
+    "bhut_tree_import": (_INT, [_VP, _VP, _VP, _I64, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                                _I64]),
     "bhut_morton_argsort_noalloc": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),
     "bhut_batch_create": (_INT, [_INT, _INT, _VP, ctypes.POINTER(_VP)]),
     "bhut_batch_configure": (_INT, [_VP, _INT, _INT, _INT, _INT]),

@@ -208,6 +208,33 @@ class TreeData:
     def num_particles(self) -> int:
         return len(self.perm)
 
+    def validate(self) -> None:
+        """Consistency checks of bhut/tree/node.py:83-134 (shapes, root count,
+        permutation, child indices, leaf sizes), same messages."""
+        M, N, D = self.num_nodes, self.num_particles, self.dim
+        if D not in (2, 3):
+            raise ValueError(f"dim must be 2 or 3, got {D}")
+        for name, arr, want in (("center", self.center, (M, D)), ("half_size", self.half_size, (M,)),
+                                ("mass", self.mass, (M,)), ("com", self.com, (M, D)),
+                                ("first_child", self.first_child, (M,)),
+                                ("child_count", self.child_count, (M,)),
+                                ("start", self.start, (M,)), ("count", self.count, (M,)),
+                                ("is_leaf", self.is_leaf, (M,))):
+            if np.shape(arr) != want:
+                raise ValueError(f"{name} has shape {np.shape(arr)}, expected {want}")
+        if np.shape(self.perm) != (N,):
+            raise ValueError(f"perm has shape {np.shape(self.perm)}, expected ({N},)")
+        if M > 0:
+            if self.count[0] != N:
+                raise ValueError(f"Root node count {self.count[0]} != num_particles {N}")
+            if not np.array_equal(np.sort(self.perm), np.arange(N)):
+                raise ValueError("perm is not a valid permutation")
+            fc = np.asarray(self.first_child)
+            if np.any(fc[fc >= 0] >= M):
+                raise ValueError("first_child indices exceed number of nodes")
+            if np.any(np.asarray(self.count)[np.asarray(self.is_leaf)] > self.leaf_size):
+                raise ValueError("Some leaf nodes exceed leaf_size")
+
     def get_children(self, node_idx: int) -> np.ndarray:
         if self.is_leaf[node_idx]:
             return np.array([], dtype=np.intp)
@@ -289,6 +316,20 @@ class _Handle:
         _sync_torch(targets, out)
         _lib.check(self.L.bhut_tree_accel_targets(self.h, _ptr(targets), int(_shape(targets)[0]),
                                                   float(theta), float(eps), float(G), _ptr(out)))
+
+    def import_tree(self, td: "TreeData", pos, m) -> None:
+        """Loads a TreeData and the particles it indexes (bhut_tree_import)."""
+        i64 = lambda a: np.ascontiguousarray(np.asarray(a), dtype=np.int64)  # noqa: E731
+        f64 = lambda a: np.ascontiguousarray(np.asarray(a), dtype=np.float64)  # noqa: E731
+        keep = (i64(td.first_child), i64(td.child_count), i64(td.start), i64(td.count),
+                i64(td.perm), f64(td.center), f64(td.half_size), f64(td.mass), f64(td.com))
+        _sync_torch(pos, m)
+        _lib.check(self.L.bhut_tree_import(self.h, _ptr(pos), _ptr(m), int(_shape(pos)[0]),
+                                           *[a.ctypes.data for a in keep], len(keep[7])))
+
+    def refit_only(self, pos, m) -> None:
+        _sync_torch(pos, m)
+        _lib.check(self.L.bhut_tree_refit_only(self.h, _ptr(pos), _ptr(m), int(_shape(pos)[0])))
 
     def export(self) -> TreeData:
         n, m, dim, L = self.info()

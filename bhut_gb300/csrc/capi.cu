@@ -474,6 +474,32 @@ int bhut_tree_refit(bhut_tree* t, const double* positions, const double* masses,
     return check_err_word(t, "refit");
 }
 
+int bhut_tree_refit_only(bhut_tree* t, const double* positions, const double* masses, int64_t n)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (!t->built) {
+        set_error("Tree must be built before refitting. Call build() first.");
+        return kNotBuilt;
+    }
+    if (n != t->n) {
+        set_error("new_positions has %lld particles but tree was built with %lld particles",
+                  (long long)n, (long long)t->n);
+        return kInvalid;
+    }
+    cudaStream_t s = t->stream;
+    BHUT_TRY(load_particles(t, positions, masses, n));
+    BHUT_TRY(launch_gather(t->pos.as<double>(), t->mass.as<double>(), t->perm.as<int32_t>(), n,
+                           t->dim, t->sx.as<double>(), t->sy.as<double>(), t->sz.as<double>(),
+                           t->sm.as<double>(), s));
+    BHUT_TRY(launch_bottom_up(t->dev(), t->leaf_list.as<int32_t>(), t->tt.num_leaves,
+                              t->first_child.as<int32_t>(), t->start.as<int32_t>(),
+                              t->count.as<int32_t>(), t->parent.as<int32_t>(),
+                              t->arrive.as<unsigned>(), t->nodes(), true, t->pos.as<double>(),
+                              t->mass.as<double>(), t->err.as<unsigned>(), s));
+    t->ff_valid = false;
+    return check_err_word(t, "refit");
+}
+
 int bhut_tree_set_form(bhut_tree* t, int form)
 {
     if (!t) { set_error("tree is NULL"); return kInvalid; }
@@ -747,6 +773,302 @@ int bhut_direct_accelerations(const double* positions, const double* masses, int
     partial.release(s);
     bhut_tree_destroy(t);
     return rc;
+}
+
+// ---- module-level stages (space/bbox.py, utils/morton.py) -------------------
+int bhut_aabb(const double* points, int64_t n, int dim, double* pmin, double* pmax, void* stream)
+{
+    if (dim < 1 || dim > 3) { set_error("dim must be 1 to 3, got %d", dim); return kInvalid; }
+    if (n <= 0) { set_error("points array cannot be empty"); return kInvalid; }
+    bhut_tree* t = nullptr;
+    BHUT_TRY(bhut_tree_create(dim == 1 ? 2 : dim, 1, stream, &t));
+    t->dim = dim;
+    cudaStream_t s = t->stream;
+    int rc = stage_in(t->pos, points, sizeof(double) * n * dim, s);
+    if (rc == kOk) rc = t->box.ensure(sizeof(double) * kBoxDoubles, s);
+    if (rc == kOk) rc = t->box_partial.ensure(sizeof(double) * kBoxPartialDoubles, s);
+    if (rc == kOk) rc = launch_bbox(t->pos.as<double>(), nullptr, n, dim, t->box_partial.as<double>(),
+                                    t->counters.as<unsigned>(), t->box.as<double>(),
+                                    t->err.as<unsigned>(), s);
+    double box[kBoxDoubles];
+    if (rc == kOk) {
+        cudaError_t e = cudaMemcpyAsync(box, t->box.p, sizeof(box), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy box");
+    }
+    // the non-finite flag of the bbox kernel is not an error here: numpy's
+    // min/max propagate NaN, and so does the copy below
+    if (rc == kOk) {
+        cudaMemsetAsync(t->err.p, 0, sizeof(unsigned), s);
+        for (int d = 0; d < dim; d++) {
+            pmin[d] = box[d];
+            pmax[d] = box[3 + d];
+        }
+    }
+    bhut_tree_destroy(t);
+    return rc;
+}
+
+int bhut_normalize_to_unit(const double* points, int64_t n, int dim, const double* pmin,
+                           const double* pmax, double eps, double* out, void* stream)
+{
+    if (dim < 1 || dim > 3) { set_error("dim must be 1 to 3, got %d", dim); return kInvalid; }
+    if (n < 0) { set_error("negative point count"); return kInvalid; }
+    if (n == 0) return kOk;
+    bhut_tree* t = nullptr;
+    BHUT_TRY(bhut_tree_create(dim == 1 ? 2 : dim, 1, stream, &t));
+    cudaStream_t s = t->stream;
+    DevBuf lim;
+    int rc = stage_in(t->pos, points, sizeof(double) * n * dim, s);
+    if (rc == kOk) rc = lim.ensure(sizeof(double) * 6, s);
+    if (rc == kOk) {
+        double h[6];
+        for (int d = 0; d < dim; d++) { h[d] = pmin[d]; h[3 + d] = pmax[d]; }
+        cudaError_t e = cudaMemcpyAsync(lim.p, h, sizeof(h), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy limits");
+    }
+    OutTarget o{nullptr, nullptr};
+    const size_t bytes = sizeof(double) * n * dim;
+    if (rc == kOk) rc = out_target(t, out, bytes, &o);
+    if (rc == kOk) rc = launch_normalize(t->pos.as<double>(), n, dim, lim.as<double>(),
+                                         lim.as<double>() + 3, 1.0 - eps, o.dev, s);
+    if (rc == kOk) rc = finish_out(t, o, bytes, "normalize_to_unit");
+    lim.release(s);
+    bhut_tree_destroy(t);
+    return rc;
+}
+
+namespace {
+// Morton codes of points in [0, 1)^dim into the handle's keys buffer.
+int unit_codes(bhut_tree* t, const double* points01, int64_t n, int dim, int bits)
+{
+    cudaStream_t s = t->stream;
+    BHUT_TRY(stage_in(t->pos, points01, sizeof(double) * n * dim, s));
+    BHUT_TRY(t->keys.ensure(sizeof(uint64_t) * n, s));
+    unsigned* bad = t->counters.as<unsigned>() + 3;
+    BHUT_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned), s));
+    BHUT_TRY(launch_morton_unit(t->pos.as<double>(), n, dim, bits, t->keys.as<uint64_t>(), bad, s));
+    unsigned h = 0;
+    BHUT_CUDA(cudaMemcpyAsync(&h, bad, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    BHUT_CUDA(cudaStreamSynchronize(s));
+    if (h) { set_error("All points must be in range [0, 1)"); return kInvalid; }
+    return kOk;
+}
+
+int check_unit_args(int64_t n, int dim, int bits)
+{
+    if (dim != 2 && dim != 3) {
+        set_error("points01 must have 2 or 3 dimensions, got %d", dim);
+        return kInvalid;
+    }
+    if (bits < 1 || bits > 62) { set_error("bits must be in 1..62, got %d", bits); return kInvalid; }
+    if (n < 0) { set_error("negative point count"); return kInvalid; }
+    return kOk;
+}
+}  // namespace
+
+int bhut_morton_codes_unit(const double* points01, int64_t n, int dim, int bits, uint64_t* codes,
+                           void* stream)
+{
+    BHUT_TRY(check_unit_args(n, dim, bits));
+    if (n == 0) return kOk;
+    bhut_tree* t = nullptr;
+    BHUT_TRY(bhut_tree_create(dim, 1, stream, &t));
+    int rc = unit_codes(t, points01, n, dim, bits);
+    if (rc == kOk) {
+        cudaError_t e = cudaMemcpyAsync(codes, t->keys.p, sizeof(uint64_t) * n, cudaMemcpyDefault,
+                                        t->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(t->stream);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy codes");
+    }
+    bhut_tree_destroy(t);
+    return rc;
+}
+
+int bhut_sort_morton_unit(const double* points01, int64_t n, int dim, int bits,
+                          uint64_t* sorted_codes, int64_t* perm, void* stream)
+{
+    BHUT_TRY(check_unit_args(n, dim, bits));
+    if (n == 0) return kOk;
+    if (n > 0x7fffffffLL) { set_error("at most 2^31-1 points are supported"); return kInvalid; }
+    bhut_tree* t = nullptr;
+    BHUT_TRY(bhut_tree_create(dim, 1, stream, &t));
+    cudaStream_t s = t->stream;
+    int rc = unit_codes(t, points01, n, dim, bits);
+    if (rc == kOk) rc = t->perm.ensure(sizeof(int32_t) * n, s);
+    if (rc == kOk) rc = t->sort_scratch.ensure(sort_scratch_bytes(n), s);
+    if (rc == kOk) rc = launch_iota(t->perm.as<int32_t>(), n, s);
+    // the interleave masks keep 21 bits per axis in 3-D, 32 in 2-D
+    const int key_bits = dim == 3 ? (3 * bits > 63 ? 63 : 3 * bits) : (2 * bits > 64 ? 64 : 2 * bits);
+    if (rc == kOk) rc = radix_sort_pairs(t->keys.as<uint64_t>(), t->perm.as<int32_t>(), n, key_bits,
+                                         t->sort_scratch.p, s);
+    if (rc == kOk && sorted_codes) {
+        cudaError_t e = cudaMemcpyAsync(sorted_codes, t->keys.p, sizeof(uint64_t) * n,
+                                        cudaMemcpyDefault, s);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy codes");
+    }
+    if (rc == kOk && perm) {
+        DevBuf p64;
+        rc = p64.ensure(sizeof(int64_t) * n, s);
+        if (rc == kOk) rc = launch_widen_i32(t->perm.as<int32_t>(), n, p64.as<int64_t>(), s);
+        if (rc == kOk) {
+            cudaError_t e = cudaMemcpyAsync(perm, p64.p, sizeof(int64_t) * n, cudaMemcpyDefault, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) rc = cuda_status(e, "copy perm");
+        }
+        p64.release(s);
+    }
+    if (rc == kOk) {
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_status(e, "sort_by_morton");
+    }
+    bhut_tree_destroy(t);
+    return rc;
+}
+
+int bhut_gather_rows(const void* src, int64_t n, int64_t row_bytes, const int64_t* perm, void* dst,
+                     void* stream)
+{
+    if (n < 0 || row_bytes < 0) { set_error("negative size"); return kInvalid; }
+    if (n == 0 || row_bytes == 0) return kOk;
+    bhut_tree* t = nullptr;
+    BHUT_TRY(bhut_tree_create(3, 1, stream, &t));
+    cudaStream_t s = t->stream;
+    DevBuf dsrc, dperm, ddst;
+    const size_t bytes = (size_t)(n * row_bytes);
+    int rc = stage_in(dsrc, src, bytes, s);
+    if (rc == kOk) rc = stage_in(dperm, perm, sizeof(int64_t) * n, s);
+    if (rc == kOk) rc = ddst.ensure(bytes, s);
+    if (rc == kOk) rc = launch_gather_rows(dsrc.p, n, row_bytes, dperm.as<int64_t>(), ddst.p,
+                                           t->err.as<unsigned>(), s);
+    if (rc == kOk) {
+        cudaError_t e = cudaMemcpyAsync(dst, ddst.p, bytes, cudaMemcpyDefault, s);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy rows");
+    }
+    if (rc == kOk) rc = check_err_word(t, "gather (permutation index out of range)");
+    for (DevBuf* b : {&dsrc, &dperm, &ddst}) b->release(s);
+    bhut_tree_destroy(t);
+    return rc;
+}
+
+int bhut_should_refit(const double* positions, int64_t n, int dim, const double* root_center,
+                      double root_half, int* refit, void* stream)
+{
+    if (dim != 2 && dim != 3) { set_error("dim must be 2 or 3, got %d", dim); return kInvalid; }
+    if (!refit) { set_error("result pointer is NULL"); return kInvalid; }
+    *refit = 1;
+    if (n <= 0) return kOk;
+    bhut_tree* t = nullptr;
+    BHUT_TRY(bhut_tree_create(dim, 1, stream, &t));
+    cudaStream_t s = t->stream;
+    DevBuf root;
+    int rc = stage_in(t->pos, positions, sizeof(double) * n * dim, s);
+    if (rc == kOk) rc = root.ensure(sizeof(double) * 4, s);
+    if (rc == kOk) {
+        double h[4] = {0, 0, 0, root_half};
+        for (int d = 0; d < dim; d++) h[d] = root_center[d];
+        cudaError_t e = cudaMemcpyAsync(root.p, h, sizeof(h), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy root");
+    }
+    unsigned* flag = t->counters.as<unsigned>() + 2;
+    if (rc == kOk) {
+        cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(unsigned), s);
+        if (e != cudaSuccess) rc = cuda_status(e, "memset");
+    }
+    if (rc == kOk) rc = launch_outside_root(t->pos.as<double>(), n, dim, root.as<double>(),
+                                            root.as<double>() + 3, flag, s);
+    unsigned outside = 0;
+    if (rc == kOk) {
+        cudaError_t e = cudaMemcpyAsync(&outside, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy flag");
+    }
+    if (rc == kOk) *refit = outside ? 0 : 1;
+    root.release(s);
+    bhut_tree_destroy(t);
+    return rc;
+}
+
+// ---- TreeData import ---------------------------------------------------------
+int bhut_tree_import(bhut_tree* t, const double* positions, const double* masses, int64_t n,
+                     const int64_t* first_child, const int64_t* child_count, const int64_t* start,
+                     const int64_t* count, const int64_t* perm, const double* center,
+                     const double* half_size, const double* mass, const double* com,
+                     int64_t num_nodes)
+{
+    if (!t) { set_error("tree is NULL"); return kInvalid; }
+    if (num_nodes <= 0 || num_nodes > 0x7fffffffLL) {
+        set_error("invalid node count %lld", (long long)num_nodes);
+        return kInvalid;
+    }
+    if (!masses) { set_error("masses are required"); return kInvalid; }
+    t->built = false;
+    t->topo_valid = false;                 // the next build recomputes its own topology
+    BHUT_TRY(load_particles(t, positions, masses, n));
+    cudaStream_t s = t->stream;
+    const int dim = t->dim;
+    const int64_t m = num_nodes;
+    DevBuf fc, cc, st, ct, pm, hf, ms, cmn, cen;
+    const size_t mi = sizeof(int64_t) * m, md = sizeof(double) * m;
+    int rc = stage_in(fc, first_child, mi, s);
+    if (rc == kOk) rc = stage_in(cc, child_count, mi, s);
+    if (rc == kOk) rc = stage_in(st, start, mi, s);
+    if (rc == kOk) rc = stage_in(ct, count, mi, s);
+    if (rc == kOk) rc = stage_in(pm, perm, sizeof(int64_t) * n, s);
+    if (rc == kOk) rc = stage_in(hf, half_size, md, s);
+    if (rc == kOk) rc = stage_in(ms, mass, md, s);
+    if (rc == kOk) rc = stage_in(cmn, com, md * dim, s);
+    if (rc == kOk) rc = stage_in(cen, center, md * dim, s);
+    for (DevBuf* b : {&t->first_child, &t->start, &t->count, &t->parent, &t->leaf_list})
+        if (rc == kOk) rc = b->ensure(sizeof(int32_t) * m, s);
+    if (rc == kOk) rc = t->cm.ensure(sizeof(NodeCM) * m, s);
+    for (DevBuf* b : {&t->size, &t->half})
+        if (rc == kOk) rc = b->ensure(sizeof(double) * m, s);
+    if (rc == kOk) rc = t->center.ensure(sizeof(double) * m * dim, s);
+    if (rc == kOk) rc = t->lo.ensure(sizeof(double) * m * 3, s);
+    if (rc == kOk) rc = t->hi.ensure(sizeof(double) * m * 3, s);
+    if (rc == kOk) rc = t->arrive.ensure(sizeof(unsigned) * m, s);
+    if (rc == kOk) rc = t->perm.ensure(sizeof(int32_t) * n, s);
+    for (DevBuf* b : {&t->sx, &t->sy, &t->sz, &t->sm})
+        if (rc == kOk) rc = b->ensure(sizeof(double) * n, s);
+    unsigned* leaves = t->counters.as<unsigned>() + 1;
+    if (rc == kOk) rc = launch_import_nodes(
+        fc.as<int64_t>(), cc.as<int64_t>(), st.as<int64_t>(), ct.as<int64_t>(), hf.as<double>(),
+        ms.as<double>(), cmn.as<double>(), cen.as<double>(), m, n, dim,
+        t->first_child.as<int32_t>(), t->start.as<int32_t>(), t->count.as<int32_t>(),
+        t->parent.as<int32_t>(), t->cm.as<NodeCM>(), t->size.as<double>(), t->half.as<double>(),
+        t->center.as<double>(), t->leaf_list.as<int32_t>(), leaves, t->err.as<unsigned>(), s);
+    if (rc == kOk) rc = launch_import_perm(pm.as<int64_t>(), n, t->perm.as<int32_t>(),
+                                           t->err.as<unsigned>(), s);
+    if (rc == kOk) rc = launch_gather(t->pos.as<double>(), t->mass.as<double>(),
+                                      t->perm.as<int32_t>(), n, dim, t->sx.as<double>(),
+                                      t->sy.as<double>(), t->sz.as<double>(), t->sm.as<double>(), s);
+    // the box of the particles frames the float-float forms
+    if (rc == kOk) rc = t->box.ensure(sizeof(double) * kBoxDoubles, s);
+    if (rc == kOk) rc = t->box_partial.ensure(sizeof(double) * kBoxPartialDoubles, s);
+    if (rc == kOk) rc = launch_bbox(t->pos.as<double>(), t->mass.as<double>(), n, dim,
+                                    t->box_partial.as<double>(), t->counters.as<unsigned>(),
+                                    t->box.as<double>(), t->err.as<unsigned>(), s);
+    unsigned nleaves = 0;
+    if (rc == kOk) {
+        cudaError_t e = cudaMemcpyAsync(&nleaves, leaves, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) rc = cuda_status(e, "copy leaf count");
+    }
+    if (rc == kOk) rc = check_err_word(t, "tree import (only binary trees with valid ranges)");
+    for (DevBuf* b : {&fc, &cc, &st, &ct, &pm, &hf, &ms, &cmn, &cen}) b->release(s);
+    if (rc != kOk) return rc;
+    t->n = n;
+    t->m = m;
+    t->tt = TopoTables{};
+    t->tt.n = -1;
+    t->tt.leaf_size = t->leaf;
+    t->tt.num_nodes = m;
+    t->tt.num_leaves = nleaves;
+    t->ff_valid = false;
+    t->built = true;
+    return kOk;
 }
 
 int bhut_tree_statistics(const double* com, const double* half_size, const double* mass,

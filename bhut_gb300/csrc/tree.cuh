@@ -181,6 +181,23 @@ int launch_tree_statistics(const StatTree& t, int dim, const double* targets, in
                            double theta, unsigned long long* totals, unsigned* err,
                            cudaStream_t s);
 
+// stages.cu
+int launch_normalize(const double* pts, int64_t n, int dim, const double* pmin, const double* pmax,
+                     double top, double* out, cudaStream_t s);
+int launch_morton_unit(const double* p01, int64_t n, int dim, int bits, uint64_t* codes,
+                       unsigned* bad, cudaStream_t s);
+int launch_gather_rows(const void* src, int64_t n, int64_t row_bytes, const int64_t* perm,
+                       void* dst, unsigned* err, cudaStream_t s);
+int launch_import_nodes(const int64_t* fc, const int64_t* cc, const int64_t* st, const int64_t* ct,
+                        const double* half_in, const double* mass_in, const double* com_in,
+                        const double* center_in, int64_t m, int64_t n, int dim,
+                        int32_t* first_child, int32_t* start, int32_t* count, int32_t* parent,
+                        NodeCM* cm, double* size, double* half, double* center,
+                        int32_t* leaf_list, unsigned* leaf_counter, unsigned* err, cudaStream_t s);
+int launch_import_perm(const int64_t* in, int64_t n, int32_t* out, unsigned* err, cudaStream_t s);
+int launch_iota(int32_t* out, int64_t n, cudaStream_t s);
+int launch_widen_i32(const int32_t* in, int64_t n, int64_t* out, cudaStream_t s);
+
 int direct_chunks(int64_t n, int64_t nt);
 int launch_direct(const double* pos, const double* mass, int64_t n, int dim, const double* targets,
                   const int64_t* self_id, int64_t nt, double eps, double G, double* out,

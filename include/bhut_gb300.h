@@ -232,6 +232,59 @@ BHUT_API int bhut_tree_statistics(const double *com, const double *half_size, co
                                   int dim, const double *targets, int64_t nt, double theta,
                                   void *stream, int64_t *totals);
 
+/* ---- module-level stages (host or device pointers; synchronous) ---------- */
+
+/* aabb (bhut/space/bbox.py:14-46): per-axis min and max of n points.
+ * NaN propagates as in numpy.  dim 1..3. */
+BHUT_API int bhut_aabb(const double *points, int64_t n, int dim, double *pmin, double *pmax,
+                       void *stream);
+
+/* normalize_to_unit (bhut/space/bbox.py:49-96): (x - pmin) / extent + offset,
+ * degenerate axes mapped to 0.5, clamped at 1 - eps.  pmin, pmax: host
+ * arrays of dim doubles. */
+BHUT_API int bhut_normalize_to_unit(const double *points, int64_t n, int dim, const double *pmin,
+                                    const double *pmax, double eps, double *out, void *stream);
+
+/* morton_codes (bhut/utils/morton.py:48-102) of points already in [0, 1)^dim,
+ * `bits` per axis (1..62); BHUT_EINVAL "All points must be in range [0, 1)"
+ * otherwise. */
+BHUT_API int bhut_morton_codes_unit(const double *points01, int64_t n, int dim, int bits,
+                                    uint64_t *codes, void *stream);
+
+/* sort_by_morton (bhut/utils/morton.py:105-147): codes of points01, stably
+ * sorted; perm (int64) = original index of each sorted point. */
+BHUT_API int bhut_sort_morton_unit(const double *points01, int64_t n, int dim, int bits,
+                                   uint64_t *sorted_codes, int64_t *perm, void *stream);
+
+/* dst[i] = src[perm[i]] for n rows of row_bytes bytes (the data_arrays of
+ * sort_by_morton, bhut/utils/morton.py:139-145). */
+BHUT_API int bhut_gather_rows(const void *src, int64_t n, int64_t row_bytes, const int64_t *perm,
+                              void *dst, void *stream);
+
+/* should_refit_vs_rebuild (bhut/tree/refit.py:195-251) boundary test: *refit
+ * = 0 when any point lies beyond 1.1 x root_half from root_center along
+ * some axis, else 1. */
+BHUT_API int bhut_should_refit(const double *positions, int64_t n, int dim,
+                               const double *root_center, double root_half, int *refit,
+                               void *stream);
+
+/* refit_tree (bhut/tree/refit.py:17-109) alone: new leaf and internal masses
+ * and centres of mass through the frozen permutation, geometry kept, no
+ * refit-vs-rebuild test (bhut_tree_refit adds that test and the rebuild). */
+BHUT_API int bhut_tree_refit_only(bhut_tree *t, const double *positions, const double *masses,
+                                  int64_t n);
+
+/* Loads a TreeData built elsewhere (bhut/tree/node.py:15-77; int64 indices,
+ * com and center as (num_nodes, dim)) with the particles it indexes, so
+ * that bhut_tree_accel_self / accel_targets / refit / export run on it
+ * (barnes_hut_accelerations bhut/traverse/bh.py:428-482, refit_tree
+ * bhut/tree/refit.py:17-109).  Binary trees only (child_count 0 or 2). */
+BHUT_API int bhut_tree_import(bhut_tree *t, const double *positions, const double *masses,
+                              int64_t n, const int64_t *first_child, const int64_t *child_count,
+                              const int64_t *start, const int64_t *count, const int64_t *perm,
+                              const double *center, const double *half_size, const double *mass,
+                              const double *com, int64_t num_nodes);
+
 #ifdef __cplusplus
 }
 #endif
