@@ -417,9 +417,12 @@ __global__ void k_bottom_up(TreeDev t, const int32_t* __restrict__ leaf_list, in
             continue;
         }
         leaf_node(id, t.dim, refit, t, opos, omass, start, count, o);
-        // climb: each step is taken by the second child to arrive
+        // climb: each step is taken by the second child to arrive; a tree
+        // deeper than kMaxClimb (or parent links with a cycle, possible in
+        // an imported TreeData) stops with an error instead of looping
         int32_t node = id;
-        while (true) {
+        for (int step = 0;; step++) {
+            if (step >= kMaxClimb) { atomicOr(err, kErrBadNode); break; }
             int32_t p = parent[node];
             if (p < 0) break;
             if (p >= t.m || first_child[p] < 1 || first_child[p] + 1 >= t.m) {
@@ -470,7 +473,8 @@ __global__ void k_quadrupoles(TreeDev t, const int32_t* __restrict__ leaf_list, 
             quad_add(q, t.sm[i], t.sx[i] - c.x, t.sy[i] - c.y, t.dim == 3 ? t.sz[i] - c.z : 0.0);
         for (int k = 0; k < 6; k++) quad[6 * (int64_t)id + k] = q[k];
         int32_t node = id;
-        while (true) {
+        for (int step = 0;; step++) {
+            if (step >= kMaxClimb) { atomicOr(err, kErrBadNode); break; }
             const int32_t p = parent[node];
             if (p < 0) break;
             if (p >= t.m || first_child[p] < 1 || first_child[p] + 1 >= t.m) {

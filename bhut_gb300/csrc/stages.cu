@@ -86,8 +86,9 @@ __global__ void k_import_nodes(const int64_t* __restrict__ fc_in, const int64_t*
             if (li < (unsigned)m) leaf_list[li] = (int32_t)k;
         } else {
             if (cc != 2 || fc < 1 || fc + 1 >= m) { atomicOr(err, kErrBadNode); continue; }
-            parent[fc] = (int32_t)k;
-            parent[fc + 1] = (int32_t)k;
+            // a node claimed by two parents makes the parent links ambiguous
+            if (atomicExch(&parent[fc], (int32_t)k) != -1) atomicOr(err, kErrBadNode);
+            if (atomicExch(&parent[fc + 1], (int32_t)k) != -1) atomicOr(err, kErrBadNode);
         }
         first_child[k] = (int32_t)fc;
         start[k] = (int32_t)st;

@@ -35,6 +35,7 @@ struct TreeDev {
 // depth d are floor(n / 2^d) or that plus one, so per depth only two count
 // values and two subtree internal-node counts exist.
 constexpr int kMaxDepth = 64;
+constexpr int kMaxClimb = 2 * kMaxDepth;   // bound of every leaf-to-root climb
 struct TopoTables {
     int depth;                     // deepest level (all nodes there are leaves)
     int64_t n;
