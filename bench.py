@@ -49,14 +49,20 @@ def _workload_desc(n, form):
 # ---------------------------------------------------------------------------
 # process group (replicas only: barrier + max of times, no data-path traffic)
 # ---------------------------------------------------------------------------
-def _dist():
+def _dist(gpu: bool = True):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch.distributed as dist
         if not dist.is_initialized():
-            dist.init_process_group("gloo")
+            # NCCL with one GPU per rank; gloo for CPU-only runs (the
+            # reference arm) or when ranks share a GPU
+            import torch
+            nccl = gpu and torch.cuda.is_available() and torch.cuda.device_count() >= ws
+            if nccl:
+                torch.cuda.set_device(local)
+            dist.init_process_group("nccl" if nccl else "gloo")
     return ws, rank, local
 
 
@@ -71,7 +77,8 @@ def _max_over_ranks(x: float, ws: int) -> float:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -134,6 +141,15 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU side: the oracle (scalar FP64 restatement of the reference's path)
 # ---------------------------------------------------------------------------
+def host_threads() -> int:
+    """Every host core this process may run on (torchrun sets
+    OMP_NUM_THREADS=1, which must not shrink the CPU baseline)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 def cpu_solve_sample(pos, m, sample_targets: int, seed: int = 0) -> dict:
     """Times the oracle on the host: full tree build (serial, as the
     reference's build) plus the traversal of a bounded random sample of
@@ -145,12 +161,14 @@ def cpu_solve_sample(pos, m, sample_targets: int, seed: int = 0) -> dict:
     t_build = time.perf_counter() - t0
     idx = np.random.default_rng(seed).choice(n, min(sample_targets, n), replace=False)
     t0 = time.perf_counter()
-    oracle.accelerations(tree, pos, m, theta=THETA, softening=EPS, G=G, self_index=idx)
+    threads = host_threads()
+    oracle.accelerations(tree, pos, m, theta=THETA, softening=EPS, G=G, self_index=idx,
+                         nthreads=threads)
     t_trav = time.perf_counter() - t0
     per_target = t_trav / len(idx)
     total = t_build + per_target * n
     return {"value": n / total, "t_build_s": t_build, "t_sample_s": t_trav,
-            "sample_targets": len(idx), "cores": oracle.num_threads()}
+            "sample_targets": len(idx), "cores": threads}
 
 
 def run_reference(args, ws, rank):
@@ -178,7 +196,7 @@ def run_reference(args, ws, rank):
         build_s.append(r["t_build_s"])
     wall = time.perf_counter() - t0
     value = float(statistics.mean(vals))
-    cores = oracle.num_threads()
+    cores = host_threads()
     desc = (f"per step: full serial tree build of N={args.n:,} plus the traversal of {sample} "
             f"random targets on {cores} threads; accels/s = N / (build time + N x per-target "
             f"traversal time)")
@@ -241,6 +259,9 @@ def run_ours(args, ws, rank, local):
     from bhut_gb300 import _lib, workloads
     from bhut_gb300.api import _Handle
 
+    # one GPU per local rank; on a node with fewer GPUs than ranks the ranks
+    # share them (replicas never wait on one another)
+    local = local % max(torch.cuda.device_count(), 1)
     torch.cuda.set_device(local)
     L = _lib.load()
     n = args.n
@@ -432,7 +453,7 @@ def main():
     if args.form is None:
         from bhut_gb300.api import DEFAULT_FORM
         args.form = DEFAULT_FORM
-    ws, rank, local = _dist()
+    ws, rank, local = _dist(gpu=args.impl != "reference")
     if args.impl == "reference":
         run_reference(args, ws, rank)
     else:
