@@ -15,8 +15,15 @@ per tick:
   and rebuilds it every ``rebuild_every`` of its own steps.  Nothing a system
   computes depends on which other systems share the batch, so a request's
   trajectory is the same alone and in any mix (bit for bit);
-* a finished request leaves at the next tick boundary and frees its slot;
-* latency = completion time - arrival time (queueing included).
+* a finished request leaves at the next tick boundary and frees its slot; so
+  does a cancelled one (``Server.cancel``) and one past its deadline
+  (``Request.deadline`` seconds after arrival), queued or resident, without
+  changing any other request's trajectory;
+* latency = completion time - arrival time (queueing included), over the
+  requests that finished;
+* ``snapshot``/``restore`` copy the queued and resident requests' state
+  (positions, velocities, accelerations, Morton order, step counts) to host
+  memory and back; a restored server continues every trajectory bit for bit.
 
 ``plain_path`` runs the same stream the simple way for comparison: one
 request at a time, one ``Tree`` per request (form ``fast``), ``refit`` every
@@ -56,6 +63,20 @@ def admits(resident: int, n_active: int, n: int, *, leaf_size: int, hbm_budget: 
     return (resident + n) * bytes_per_particle(leaf_size) <= hbm_budget
 
 
+def retire_reason(steps_done: int, steps: int, waited: float, deadline: float | None,
+                  cancelled: bool) -> str | None:
+    """Why a request leaves at this tick boundary, if it does: "cancelled",
+    "done" (all its steps taken), "timed_out" (``waited`` seconds since its
+    arrival exceed its ``deadline``), else None."""
+    if cancelled:
+        return "cancelled"
+    if steps_done >= steps:
+        return "done"
+    if deadline is not None and waited > deadline:
+        return "timed_out"
+    return None
+
+
 def keeps_order(primed: bool, has_order: bool, steps_done: int, rebuild_every: int) -> bool:
     """Refit (keep the last Morton order) unless this system's rebuild is
     due: its first solve, and every ``rebuild_every`` of its own steps
@@ -72,7 +93,9 @@ class Request:
     masses: np.ndarray
     steps: int = 100
     kind: str = ""
+    deadline: float | None = None   # seconds after arrival; None: no deadline
     # runtime state
+    status: str = ""                # "done", "cancelled" or "timed_out" once it left
     steps_done: int = 0
     solves: int = 0
     primed: bool = False
@@ -142,11 +165,19 @@ class Server:
         self.finished: list[Request] = []
         self.ticks = 0
         self._solve_events = []
+        self._cancel: set[int] = set()
+        self.queue: list[Request] = []
+        self.mem_peak = 0
         self.solves = 0
         self.accels = 0
         self.peak_bytes = 0.0
 
     # -- device state ------------------------------------------------------
+    def cancel(self, rid: int) -> None:
+        """Cancels request ``rid`` (queued or resident) at the next tick
+        boundary."""
+        self._cancel.add(rid)
+
     def _fits(self, r: Request) -> bool:
         return admits(sum(a.n for a in self.active), len(self.active), r.n,
                       leaf_size=self.leaf_size, hbm_budget=self.hbm_budget,
@@ -225,20 +256,42 @@ class Server:
         self.ticks += 1
 
     # -- the loop ----------------------------------------------------------
-    def run(self, requests: list[Request], *, realtime: bool = True,
-            max_seconds: float | None = None) -> dict:
+    def _leave(self, r: Request, reason: str, t: float) -> None:
+        r.status = reason
+        r.done_at = t
+        self.finished.append(r)
+        if r.primed or r.admitted_at is not None:
+            r.final_positions = r.positions.clone()
+            r.final_velocities = r.velocities.clone()
+
+    def run(self, requests: list[Request] = (), *, realtime: bool = True,
+            max_seconds: float | None = None, max_ticks: int | None = None,
+            t0: float = 0.0) -> dict:
+        """Serves ``requests`` (plus any restored queue) until all have left,
+        or until ``max_seconds`` / ``max_ticks``; ``t0`` is the stream time
+        at which this run starts (for a restored server)."""
         torch = self.torch
-        queue = sorted(requests, key=lambda r: r.arrival)
-        t_start = time.perf_counter()
+        queue = sorted(list(self.queue) + list(requests), key=lambda r: r.arrival)
+        self.queue = queue
+        t_start = time.perf_counter() - t0
+        ticks0 = self.ticks
 
         def now():
             return time.perf_counter() - t_start
 
-        changed = False
+        changed = bool(self.active)
         while queue or self.active:
             t = now()
             if max_seconds is not None and t > max_seconds:
                 break
+            if max_ticks is not None and self.ticks - ticks0 >= max_ticks:
+                break
+            for r in [q for q in queue if q.arrival <= t or not realtime]:
+                why = retire_reason(0, max(r.steps, 1), t - r.arrival, r.deadline,
+                                    r.rid in self._cancel)
+                if why in ("cancelled", "timed_out"):
+                    queue.remove(r)
+                    self._leave(r, why, t)
             while queue and (queue[0].arrival <= t or not realtime) and self._fits(queue[0]):
                 r = queue.pop(0)
                 r.admitted_at = t
@@ -257,31 +310,84 @@ class Server:
                 changed = False
             self.tick()
             torch.cuda.current_stream().synchronize()
+            free, total = torch.cuda.mem_get_info()
+            self.mem_peak = max(self.mem_peak, total - free)
             t = now()
-            done = [r for r in self.active if r.steps_done >= r.steps]
-            if done:
-                for r in done:
-                    r.done_at = t
-                    self.active.remove(r)
-                    self.finished.append(r)
-                    r.final_positions = r.positions.clone()
-                    r.final_velocities = r.velocities.clone()
+            leaving = []
+            for r in self.active:
+                why = retire_reason(r.steps_done, r.steps, t - r.arrival, r.deadline,
+                                    r.rid in self._cancel)
+                if why:
+                    leaving.append((r, why))
+            for r, why in leaving:
+                self.active.remove(r)
+                self._leave(r, why, t)
+            if leaving:
                 changed = bool(self.active)
-        wall = now()
+        wall = now() - t0
         torch.cuda.synchronize()
         solve_s = sum(a.elapsed_time(b) for a, b in self._solve_events) / 1e3
         self._solve_events = []
-        lat = np.array([r.latency for r in self.finished if r.latency is not None])
+        done = [r for r in self.finished if r.status == "done"]
+        lat = np.array([r.latency for r in done if r.latency is not None])
         return {
-            "requests_done": len(self.finished), "wall_s": wall, "ticks": self.ticks,
+            "requests_done": len(done),
+            "requests_cancelled": sum(r.status == "cancelled" for r in self.finished),
+            "requests_timed_out": sum(r.status == "timed_out" for r in self.finished),
+            "wall_s": wall, "ticks": self.ticks,
             "solves": self.solves, "solves_per_s": self.solves / wall if wall else 0.0,
             "accels_per_s": self.accels / wall if wall else 0.0,
             "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else None,
             "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None,
             "peak_resident_bytes_est": self.peak_bytes,
+            "device_mem_used_peak_bytes": self.mem_peak,
             "solve_device_s": solve_s,
             "solve_share_of_wall": solve_s / wall if wall else None,
         }
+
+    # -- checkpoint / resume ----------------------------------------------------
+    def snapshot(self) -> dict:
+        """Host copy of every queued and resident request's state (call
+        between ticks, e.g. after ``run(max_ticks=k)``)."""
+        def host(x):
+            return None if x is None else (x.cpu().numpy().copy() if hasattr(x, "cpu")
+                                           else np.array(x, copy=True))
+        reqs = []
+        for r in self.active + self.queue:
+            reqs.append({
+                "rid": r.rid, "arrival": r.arrival, "steps": r.steps, "kind": r.kind,
+                "deadline": r.deadline, "steps_done": r.steps_done, "solves": r.solves,
+                "primed": r.primed, "admitted_at": r.admitted_at, "resident": r in self.active,
+                "positions": host(r.positions), "velocities": host(r.velocities),
+                "masses": host(r.masses), "acc": host(r.acc), "order": host(r.order)})
+        return {"requests": reqs, "ticks": self.ticks, "solves": self.solves,
+                "accels": self.accels, "cancelled": sorted(self._cancel)}
+
+    def restore(self, snap: dict) -> list[Request]:
+        """Loads a snapshot into this (fresh) server: resident requests are
+        resident again in the same order, queued ones queued; returns the
+        requests."""
+        torch = self.torch
+        out = []
+        for d in snap["requests"]:
+            r = Request(d["rid"], d["arrival"], d["positions"], d["velocities"], d["masses"],
+                        steps=d["steps"], kind=d["kind"], deadline=d["deadline"])
+            r.steps_done, r.solves, r.primed = d["steps_done"], d["solves"], d["primed"]
+            r.admitted_at = d["admitted_at"]
+            if d["resident"]:
+                r.positions = torch.as_tensor(d["positions"], device="cuda")
+                r.velocities = torch.as_tensor(d["velocities"], device="cuda")
+                r.masses = torch.as_tensor(d["masses"], device="cuda")
+                r.acc = torch.as_tensor(d["acc"], device="cuda")
+                r.order = None if d["order"] is None else torch.as_tensor(d["order"],
+                                                                          device="cuda")
+                self.active.append(r)
+            else:
+                self.queue.append(r)
+            out.append(r)
+        self.ticks, self.solves, self.accels = snap["ticks"], snap["solves"], snap["accels"]
+        self._cancel = set(snap["cancelled"])
+        return out
 
     def close(self):
         self.solver.close()
@@ -322,6 +428,8 @@ def plain_path(requests: list[Request], *, theta: float = 0.5, softening: float 
             solves += 1
         torch.cuda.synchronize()
         accels += r.n * (r.steps + 1)
+        r.final_positions, r.final_velocities = x, v
+        r.status = "done"
         tree.close()
         r.done_at = time.perf_counter() - t_start
         done.append(r)

@@ -48,11 +48,17 @@ def test_server_matches_plain_integration_within_tolerance():
     r2 = _req(0, 4000, 5, steps=10)
     serve.plain_path([r2], theta=0.5, softening=0.01, dt=1e-3, rebuild_every=5,
                      realtime=False)
-    # the plain path refits with the reference's stale boxes; positions after
-    # 10 steps of dt=1e-3 still agree to ~1e-8 of their spread
+    # different arithmetic (FP32 + quadrupoles vs float-float monopoles) and
+    # refit geometry: the trajectories differ by the Barnes-Hut truncation
+    # error (~1e-3 of a) acting for 10 steps of dt=1e-3, far below the
+    # distance the particles moved (~1e-3)
     assert r2.done_at is not None
     x1 = r1.final_positions.cpu().numpy()
+    x2 = r2.final_positions.cpu().numpy()
     assert np.all(np.isfinite(x1))
+    moved = np.linalg.norm(x2 - _req(0, 4000, 5).positions, axis=1).mean()
+    diff = np.linalg.norm(x1 - x2, axis=1)
+    assert diff.mean() < 1e-3 * moved and diff.max() < 0.2 * moved
 
 
 def test_admission_budget():
@@ -63,3 +69,39 @@ def test_admission_budget():
     assert st["requests_done"] == 3
     # never more than one system resident at a time under this budget
     assert st["peak_resident_bytes_est"] <= 2500 * serve.bytes_per_particle(16)
+
+
+def test_cancel_and_deadline_leave_others_unchanged():
+    alone = _req(0, 3000, 1)
+    _run([alone])
+    mix = [_req(0, 3000, 1), _req(1, 2000, 2, steps=50), _req(2, 1500, 3, steps=50),
+           _req(3, 800, 4, steps=5)]
+    mix[2].deadline = 0.0          # times out at the first tick boundary
+    sv = serve.Server(theta=0.5, softening=0.01, dt=1e-3, rebuild_every=5)
+    sv.cancel(1)
+    st = sv.run(mix, realtime=False)
+    sv.close()
+    assert [r.status for r in mix] == ["done", "cancelled", "timed_out", "done"]
+    assert st["requests_done"] == 2 and st["requests_cancelled"] == 1
+    assert st["requests_timed_out"] == 1 and st["device_mem_used_peak_bytes"] > 0
+    assert np.array_equal(mix[0].final_positions.cpu().numpy(),
+                          alone.final_positions.cpu().numpy())
+
+
+def test_snapshot_restore_continues_bit_for_bit():
+    ref = [_req(0, 3000, 1, steps=9), _req(1, 1200, 2, steps=14)]
+    _run(ref)
+    reqs = [_req(0, 3000, 1, steps=9), _req(1, 1200, 2, steps=14)]
+    sv = serve.Server(theta=0.5, softening=0.01, dt=1e-3, rebuild_every=5)
+    sv.run(reqs, realtime=False, max_ticks=6)     # stop mid-run (a rebuild is due at 5)
+    snap = sv.snapshot()
+    sv.close()
+    sv2 = serve.Server(theta=0.5, softening=0.01, dt=1e-3, rebuild_every=5)
+    back = sv2.restore(snap)
+    sv2.run(realtime=False)
+    sv2.close()
+    for a, b in zip(sorted(back, key=lambda r: r.rid), ref):
+        assert a.status == "done" and a.steps_done == b.steps_done
+        assert np.array_equal(a.final_positions.cpu().numpy(), b.final_positions.cpu().numpy())
+        assert np.array_equal(a.final_velocities.cpu().numpy(),
+                              b.final_velocities.cpu().numpy())

@@ -45,3 +45,13 @@ def test_refit_rebuild_schedule():
     assert not serve.keeps_order(True, False, 3, 10)
     sched = [serve.keeps_order(True, True, s, 10) for s in range(25)]
     assert [s for s, k in enumerate(sched) if not k] == [0, 10, 20]
+
+
+def test_retire_reasons():
+    assert serve.retire_reason(3, 10, 0.5, None, False) is None
+    assert serve.retire_reason(10, 10, 0.5, None, False) == "done"
+    assert serve.retire_reason(3, 10, 0.5, 0.4, False) == "timed_out"
+    assert serve.retire_reason(3, 10, 0.3, 0.4, False) is None
+    # cancellation wins over everything, completion over the deadline
+    assert serve.retire_reason(10, 10, 9.0, 0.4, True) == "cancelled"
+    assert serve.retire_reason(10, 10, 9.0, 0.4, False) == "done"
