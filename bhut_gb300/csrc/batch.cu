@@ -498,12 +498,15 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                 float4 nhv = make_float4(0.f, 0.f, 0.f, 0.f), nlv = nhv;
                 if (act) {
                     nhv = b.nh[node];
-                    nlv = b.nl[node];
+                    if (!FP32) nlv = b.nl[node];
                     float d2 = 0.0f;
 #pragma unroll
                     for (int k = 0; k < DIM; k++) {
-                        const float d = __fadd_rn(__fsub_rn(comp(nhv, k), Th[k]),
-                                                  __fsub_rn(comp(nlv, k), Tl[k]));
+                        // FP32 form: hi coordinates only (exact differences),
+                        // as the single-tree FP32 walk
+                        const float d = FP32 ? __fsub_rn(comp(nhv, k), Th[k])
+                                             : __fadd_rn(__fsub_rn(comp(nhv, k), Th[k]),
+                                                         __fsub_rn(comp(nlv, k), Tl[k]));
                         d2 = fmaf(d, d, d2);
                     }
                     const float dist = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
@@ -525,6 +528,7 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                 const unsigned omask = __ballot_sync(FULL, act && open);
                 if (act && !open && sub == 0) {
                     if (FP32) {
+                        nlv = b.nl[node];
                         if (b.nq0)
                             node_quad_f32<DIM>(Th, Tl, nhv, nlv, b.nq0[node], b.nq1[node], e2h,
                                                ah, al);

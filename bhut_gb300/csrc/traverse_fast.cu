@@ -397,13 +397,14 @@ __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, c
             bool open = false;
             float4 nh = make_float4(0.f, 0.f, 0.f, 0.f);
             if (act) {
+                // opening test on the hi coordinates (exact differences on
+                // the 2^-23 grid): the FP32 form's criterion is a heuristic,
+                // so a decision at the margin may go either way
                 nh = ft.nh[node];
-                const float4 nlo = ft.nl[node];
                 float d2 = 0.0f;
 #pragma unroll
                 for (int k = 0; k < DIM; k++) {
-                    const float d = __fadd_rn(__fsub_rn(comp(nh, k), T[k]),
-                                              __fsub_rn(comp(nlo, k), Tl[k]));
+                    const float d = __fsub_rn(comp(nh, k), T[k]);
                     d2 = fmaf(d, d, d2);
                 }
                 const float dist = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
