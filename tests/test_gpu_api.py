@@ -118,3 +118,26 @@ def test_2d_and_leaf_sizes(oracle_mod):
         ot = oracle_mod.build_tree(pos, m, L)
         ref = oracle_mod.accelerations(ot, pos, m, theta=0.6, softening=0.02)
         assert rel_l2(acc, ref) <= 1e-11, L
+
+
+@pytest.mark.parametrize("form", ["exact", "fast", "fp32"])
+def test_two_body_extremes(form, oracle_mod):
+    """The reference's numerical edge cases (tests/edge_cases, two bodies,
+    softening 0): coincident points, 1e-15 and 1e15 separations, 1e-15 and
+    1e10 masses, 1e12 offsets with unit separation."""
+    cases = [
+        (np.array([[1.0, 2.0, 3.0], [1.0, 2.0, 3.0]]), np.array([1.0, 1.0])),
+        (np.array([[0.0, 0.0, 0.0], [1e-15, 0.0, 0.0]]), np.array([1.0, 1.0])),
+        (np.array([[0.0, 0.0, 0.0], [1e15, 0.0, 0.0]]), np.array([1.0, 1.0])),
+        (np.array([[0.0, 0.0, 0.0], [1e6, 0.0, 0.0]]), np.array([1e-15, 1e-15])),
+        (np.array([[0.0, 0.0, 0.0], [1e-6, 0.0, 0.0]]), np.array([1e10, 1e10])),
+        (np.array([[1e12, 1e12, 1e12], [1e12 + 1.0, 1e12, 1e12]]), np.array([1.0, 1.0])),
+    ]
+    tol = {"exact": 1e-15, "fast": 1e-13, "fp32": 1e-6}[form]
+    for pos, m in cases:
+        acc = bh.accelerations(pos, m, form=form)
+        ref = oracle_mod.accelerations(oracle_mod.build_tree(pos, m, 32), pos, m, theta=0.5,
+                                       softening=0.0)
+        assert np.all(np.isfinite(acc))
+        assert np.allclose(acc, ref, rtol=tol, atol=0.0), (form, pos, acc, ref)
+        assert np.allclose(acc[0], -acc[1] * m[1] / m[0], rtol=1e-12 if form != "fp32" else 1e-6)
