@@ -1071,6 +1071,12 @@ int bhut_tree_import(bhut_tree* t, const double* positions, const double* masses
     return kOk;
 }
 
+int bhut_measure_fp32_peak(double* tflops)
+{
+    if (!tflops) { set_error("result pointer is NULL"); return kInvalid; }
+    return measure_fp32_peak(tflops);
+}
+
 int bhut_tree_statistics(const double* com, const double* half_size, const double* mass,
                          const int64_t* first_child, const int64_t* child_count,
                          const int64_t* start, const int64_t* count, int64_t num_nodes, int dim,

@@ -202,3 +202,57 @@ int launch_import_perm(const int64_t* in, int64_t n, int32_t* out, unsigned* err
 }
 
 }  // namespace bhut
+
+// ---------------------------------------------------------------------------
+// FP32 pipe peak: independent FMA chains (16 per thread), the denominator of
+// the FP32-pipe rooflines next to the cuBLAS SGEMM figure.
+// ---------------------------------------------------------------------------
+namespace bhut {
+
+__global__ void k_fma_peak(float* __restrict__ out, int iters, float m, float c)
+{
+    float a[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) a[j] = threadIdx.x * 1e-3f + (float)j;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) a[j] = fmaf(a[j], m, c);
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 16; j++) s += a[j];
+    out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = s;
+}
+
+int measure_fp32_peak(double* tflops)
+{
+    int dev = 0, sms = 0;
+    BHUT_CUDA(cudaGetDevice(&dev));
+    BHUT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8, threads = 256, iters = 20000;
+    float* out = nullptr;
+    BHUT_CUDA(cudaMalloc(&out, sizeof(float) * blocks * threads));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int r = 0; r < 3; r++) {
+        cudaEventRecord(e0);
+        k_fma_peak<<<blocks, threads>>>(out, iters, 0.999f, 1e-3f);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0 && ms < best) best = ms;
+    }
+    note_launches(3);
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess) return cuda_status(e, "fp32 peak kernel");
+    *tflops = 2.0 * 16.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+    return kOk;
+}
+
+}  // namespace bhut

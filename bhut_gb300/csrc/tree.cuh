@@ -198,6 +198,7 @@ int launch_import_nodes(const int64_t* fc, const int64_t* cc, const int64_t* st,
 int launch_import_perm(const int64_t* in, int64_t n, int32_t* out, unsigned* err, cudaStream_t s);
 int launch_iota(int32_t* out, int64_t n, cudaStream_t s);
 int launch_widen_i32(const int32_t* in, int64_t n, int64_t* out, cudaStream_t s);
+int measure_fp32_peak(double* tflops);
 
 int direct_chunks(int64_t n, int64_t nt);
 int launch_direct(const double* pos, const double* mass, int64_t n, int dim, const double* targets,

@@ -285,6 +285,11 @@ BHUT_API int bhut_tree_import(bhut_tree *t, const double *positions, const doubl
                               const double *center, const double *half_size, const double *mass,
                               const double *com, int64_t num_nodes);
 
+/* Measured FP32 FMA peak of the current GPU (TFLOP/s): independent FMA
+ * chains on every SM, best of 2 timed runs.  A measurement utility for the
+ * FP32-pipe rooflines; no reference counterpart. */
+BHUT_API int bhut_measure_fp32_peak(double *tflops);
+
 #ifdef __cplusplus
 }
 #endif
