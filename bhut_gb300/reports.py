@@ -3,6 +3,7 @@
     python -m bhut_gb300.reports precision [--n 4000000] [--sample 8192]
     python -m bhut_gb300.reports batched [--nsys 2048]
     python -m bhut_gb300.reports served [--count 24] [--theta 0.7]
+    python -m bhut_gb300.reports scaling [--sizes 1e5,1e6,4e6,16e6,64e6]
 
 ``precision``: the galaxy model (70 % exponential disc, 30 % Hernquist bulge,
 equal masses), softening 0.005, theta in {0.3, 0.5, 0.7}.  For each theta the
@@ -263,9 +264,52 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
     return line
 
 
+def scaling_report(sizes=(100_000, 1_000_000, 4_000_000, 16_000_000, 64_000_000),
+                   forms=("fast", "fp32"), theta: float = 0.5, eps: float = 0.01, reps: int = 2):
+    """``scaling``: self accelerations of Plummer spheres of growing N
+    (theta 0.5, eps 0.01, leaf 32), build and traversal timed separately
+    through one persistent tree handle; accels/s and interactions per
+    target for each form."""
+    import torch
+    from .api import _Handle
+    lines = []
+    for n in sizes:
+        pos, m = workloads.plummer(int(n), seed=3)
+        pd, md = torch.as_tensor(pos).cuda(), torch.as_tensor(m).cuda()
+        out = torch.empty_like(pd)
+        for form in forms:
+            h = _Handle(3, 32)
+            h.set_form(form)
+            best_b = best_t = float("inf")
+            for r in range(reps + 1):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                h.build(pd, md)
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                h.accel_self(theta, eps, 1.0, out)
+                torch.cuda.synchronize()
+                t2 = time.perf_counter()
+                if r:
+                    best_b, best_t = min(best_b, t1 - t0), min(best_t, t2 - t1)
+            p2p, m2p, visits = h.stats()
+            h.close()
+            line = {"report": "scaling", "n": int(n), "form": form, "theta": theta,
+                    "build_ms": best_b * 1e3, "traversal_ms": best_t * 1e3,
+                    "accels_per_s": n / (best_b + best_t),
+                    "p2p_per_target": p2p / n, "m2p_per_target": m2p / n,
+                    "visits_per_target": visits / n}
+            _log(f"N={n:,} {form}: {line['accels_per_s']:.3g} accels/s")
+            print(json.dumps(line), flush=True)
+            lines.append(line)
+        del pd, md, out
+    return lines
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("report", choices=["precision", "batched", "served"])
+    ap.add_argument("report", choices=["precision", "batched", "served", "scaling"])
+    ap.add_argument("--sizes", default="1e5,1e6,4e6,16e6,64e6")
     ap.add_argument("--count", type=int, default=24)
     ap.add_argument("--nsys", type=int, default=2048)
     ap.add_argument("--n", type=int, default=4_000_000)
@@ -284,6 +328,8 @@ def main():
         batched_report(args.nsys, criterion=args.criterion or "bh",
                        multipole=args.multipole or "mono",
                        theta=args.theta if args.theta is not None else 0.5)
+    elif args.report == "scaling":
+        scaling_report(tuple(int(float(x)) for x in args.sizes.split(",")))
     elif args.report == "served":
         served_report(args.count, criterion=args.criterion or "bh_offset",
                       multipole=args.multipole or "quad",
