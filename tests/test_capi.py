@@ -53,3 +53,30 @@ def test_invalid_arguments_rejected_before_device_work(engine_lib):
     assert L.bhut_tree_create(3, 0, None, ctypes.byref(h)) == _lib.BHUT_EINVAL
     assert "leaf_size must be positive" in _lib.last_error()
     assert L.bhut_morton_keys(None, 0, 3, None, None) == _lib.BHUT_EINVAL
+
+
+def test_more_invalid_arguments(engine_lib):
+    """Argument checks of the newer entry points, before any device work."""
+    from bhut_gb300 import _lib
+    L = _lib.load()
+    E = _lib.BHUT_EINVAL
+    assert L.bhut_batch_configure(None, 2, 0, 32, 1) == E
+    assert L.bhut_batch_set_multipole(None, 1) == E
+    assert L.bhut_batch_set_stack(None, 1) == E
+    assert L.bhut_tree_set_multipole(None, 0) == E
+    assert L.bhut_tree_set_criterion(None, 0) == E
+    assert L.bhut_morton_codes_unit(None, 10, 4, 21, None, None) == E
+    assert "points01 must have 2 or 3 dimensions" in _lib.last_error()
+    assert L.bhut_morton_codes_unit(None, 10, 3, 0, None, None) == E
+    assert "bits must be in 1..62" in _lib.last_error()
+    assert L.bhut_sort_morton_unit(None, 10, 3, 63, None, None, None) == E
+    assert L.bhut_gather_rows(None, -1, 8, None, None, None) == E
+    assert L.bhut_should_refit(None, 10, 4, None, 1.0, None, None) == E
+    assert L.bhut_tree_statistics(None, None, None, None, None, None, None, 0, 3, None, 0, 0.5,
+                                  None, None) == E
+    assert L.bhut_tree_import(None, None, None, 0, None, None, None, None, None, None, None,
+                              None, None, 0) == E
+    assert L.bhut_tree_refit_only(None, None, None, 0) == E
+    assert L.bhut_measure_fp32_peak(None) == E
+    assert L.bhut_aabb(None, 0, 3, None, None, None) == E
+    assert "points array cannot be empty" in _lib.last_error()
