@@ -70,6 +70,8 @@ SIGNATURES = {
     "bhut_should_refit": (_INT, [_VP, _I64, _INT, _VP, _D, _VP, _VP]),
     "bhut_tree_refit_only": (_INT, [_VP, _VP, _VP, _I64]),
     "bhut_measure_fp32_peak": (_INT, [_VP]),
+    "bhut_pool_usage": (_INT, [_VP, _VP]),
+    "bhut_pool_trim": (_INT, []),
     "bhut_tree_import": (_INT, [_VP, _VP, _VP, _I64, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
                                 _I64]),
     "bhut_morton_argsort_noalloc": (_INT, [_VP, _I64, _INT, _VP, _VP, _VP]),

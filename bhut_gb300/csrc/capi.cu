@@ -1071,6 +1071,32 @@ int bhut_tree_import(bhut_tree* t, const double* positions, const double* masses
     return kOk;
 }
 
+int bhut_pool_usage(int64_t* used, int64_t* reserved)
+{
+    if (!used || !reserved) { set_error("result pointer is NULL"); return kInvalid; }
+    int dev = 0;
+    BHUT_CUDA(cudaGetDevice(&dev));
+    cudaMemPool_t pool;
+    BHUT_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    unsigned long long u = 0, r = 0;   // the attributes are 64-bit counts
+    BHUT_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &u));
+    BHUT_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r));
+    *used = (int64_t)u;
+    *reserved = (int64_t)r;
+    return kOk;
+}
+
+int bhut_pool_trim(void)
+{
+    int dev = 0;
+    BHUT_CUDA(cudaGetDevice(&dev));
+    cudaMemPool_t pool;
+    BHUT_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    BHUT_CUDA(cudaDeviceSynchronize());
+    BHUT_CUDA(cudaMemPoolTrimTo(pool, 0));
+    return kOk;
+}
+
 int bhut_measure_fp32_peak(double* tflops)
 {
     if (!tflops) { set_error("result pointer is NULL"); return kInvalid; }

@@ -6,8 +6,10 @@ system's state in HBM and advances all of them together, one batched solve
 per tick:
 
 * admission: a queued request is admitted at a tick boundary once it has
-  arrived and its estimated device footprint fits the HBM budget (and the
-  optional cap on resident particles);
+  arrived and its device footprint (``bytes_per_particle``: the buffers
+  counted, plus a measured allocator margin) fits the HBM budget (and the
+  optional cap on resident particles); a request that does not fit even on an
+  empty server is rejected;
 * each tick: first half-kick and drift (``bhut_leapfrog``), one batched
   solve of every resident system (``bhut_batch_*``), second half-kick;
 * each system refits its tree on its own schedule -- its Morton order is kept
@@ -39,16 +41,28 @@ import numpy as np
 from . import _lib, api, workloads
 from .batch import BatchedSolver
 
-# Device bytes per resident particle: request state (x, v, a, m, order),
-# the batch's copies, sort scratch and float-float particles, and the node
-# arrays (about 2 N / leaf_size nodes of ~190 B, plus 72 B of quadrupoles).
-STATE_BYTES = 3 * 24 + 8 + 4
-BATCH_BYTES = 24 + 8 + 8 + 8 + 4 + 4 + 32 + 32 + 12 + 4 + 24
-NODE_BYTES = 262
+# Device bytes per resident particle, counted from the buffers:
+#  request state: x, v, a (3 x 24), m (8), last Morton order (4), and the same
+#    again while the packed arrays are rebuilt after an admission/retirement;
+#  batch: positions and masses copies (32), keys, second keys (16), perm and
+#    system ids (8), sorted SoA (32), float-float copies (32), sort scratch
+#    (12), kept-order and tick permutations (12);
+#  nodes: about 2 N / leaf_size of 268 B (centre of mass and mass 32, size,
+#    half, centre, AABB scratch 88, topology links 20, float-float copies and
+#    header 56, quadrupoles and their float copies 72).
+STATE_BYTES = 2 * (3 * 24 + 8 + 4)
+BATCH_BYTES = 32 + 16 + 8 + 32 + 32 + 12 + 12
+NODE_BYTES = 268
+# allocator granularity, buffers kept at their largest layout and the copies
+# made while repacking, on top of the buffer count: measured 1.16x at a steady
+# 3.1M resident particles and 1.87x over a 100-request stream with admissions
+# and retirements every few ticks (device memory above the server's start,
+# leaf 16)
+FOOTPRINT_MARGIN = 2.0
 
 
 def bytes_per_particle(leaf_size: int) -> float:
-    return STATE_BYTES + BATCH_BYTES + 2.0 * NODE_BYTES / leaf_size
+    return FOOTPRINT_MARGIN * (STATE_BYTES + BATCH_BYTES + 2.0 * NODE_BYTES / leaf_size)
 
 
 def admits(resident: int, n_active: int, n: int, *, leaf_size: int, hbm_budget: float,
@@ -95,7 +109,7 @@ class Request:
     kind: str = ""
     deadline: float | None = None   # seconds after arrival; None: no deadline
     # runtime state
-    status: str = ""                # "done", "cancelled" or "timed_out" once it left
+    status: str = ""                # "done", "cancelled", "timed_out" or "rejected" once it left
     steps_done: int = 0
     solves: int = 0
     primed: bool = False
@@ -168,6 +182,11 @@ class Server:
         self._cancel: set[int] = set()
         self.queue: list[Request] = []
         self.mem_peak = 0
+        # device memory in use before any request state (the reported peak
+        # is measured against it)
+        torch.cuda.synchronize()
+        free, total = torch.cuda.mem_get_info()
+        self.mem_base = total - free
         self.solves = 0
         self.accels = 0
         self.peak_bytes = 0.0
@@ -261,8 +280,9 @@ class Server:
         r.done_at = t
         self.finished.append(r)
         if r.primed or r.admitted_at is not None:
-            r.final_positions = r.positions.clone()
-            r.final_velocities = r.velocities.clone()
+            # the response goes to host memory and frees its device slot
+            r.final_positions = r.positions.to("cpu")
+            r.final_velocities = r.velocities.to("cpu")
 
     def run(self, requests: list[Request] = (), *, realtime: bool = True,
             max_seconds: float | None = None, max_ticks: int | None = None,
@@ -295,23 +315,29 @@ class Server:
             while queue and (queue[0].arrival <= t or not realtime) and self._fits(queue[0]):
                 r = queue.pop(0)
                 r.admitted_at = t
-                r.positions = torch.as_tensor(np.asarray(r.positions), device="cuda").clone()
-                r.velocities = torch.as_tensor(np.asarray(r.velocities), device="cuda").clone()
-                r.masses = torch.as_tensor(np.asarray(r.masses), device="cuda").clone()
+                r.positions = torch.tensor(np.asarray(r.positions), device="cuda")
+                r.velocities = torch.tensor(np.asarray(r.velocities), device="cuda")
+                r.masses = torch.tensor(np.asarray(r.masses), device="cuda")
                 r.acc = torch.zeros_like(r.positions)
                 self.active.append(r)
                 changed = True
             if not self.active:
-                if queue and realtime:
+                if queue and (queue[0].arrival <= t or not realtime):
+                    # it does not fit even on an empty server: reject it
+                    # rather than wait for room that never comes
+                    self._leave(queue.pop(0), "rejected", t)
+                elif queue and realtime:
                     time.sleep(max(0.0, min(queue[0].arrival - t, 0.05)))
                 continue
             if changed:
                 self._pack()
                 changed = False
+                torch.cuda.empty_cache()   # the pre-pack copies go back to the device
             self.tick()
             torch.cuda.current_stream().synchronize()
             free, total = torch.cuda.mem_get_info()
             self.mem_peak = max(self.mem_peak, total - free)
+
             t = now()
             leaving = []
             for r in self.active:
@@ -324,6 +350,11 @@ class Server:
                 self._leave(r, why, t)
             if leaving:
                 changed = bool(self.active)
+                if changed:
+                    self._pack()          # drop the retired systems' state now
+                    changed = False
+                torch.cuda.empty_cache()  # and hand their blocks back
+                _lib.check(self.L.bhut_pool_trim())
         wall = now() - t0
         torch.cuda.synchronize()
         solve_s = sum(a.elapsed_time(b) for a, b in self._solve_events) / 1e3
@@ -334,6 +365,7 @@ class Server:
             "requests_done": len(done),
             "requests_cancelled": sum(r.status == "cancelled" for r in self.finished),
             "requests_timed_out": sum(r.status == "timed_out" for r in self.finished),
+            "requests_rejected": sum(r.status == "rejected" for r in self.finished),
             "wall_s": wall, "ticks": self.ticks,
             "solves": self.solves, "solves_per_s": self.solves / wall if wall else 0.0,
             "accels_per_s": self.accels / wall if wall else 0.0,
@@ -341,6 +373,7 @@ class Server:
             "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None,
             "peak_resident_bytes_est": self.peak_bytes,
             "device_mem_used_peak_bytes": self.mem_peak,
+            "device_mem_request_peak_bytes": self.mem_peak - self.mem_base,
             "solve_device_s": solve_s,
             "solve_share_of_wall": solve_s / wall if wall else None,
         }
@@ -428,7 +461,7 @@ def plain_path(requests: list[Request], *, theta: float = 0.5, softening: float 
             solves += 1
         torch.cuda.synchronize()
         accels += r.n * (r.steps + 1)
-        r.final_positions, r.final_velocities = x, v
+        r.final_positions, r.final_velocities = x.to("cpu"), v.to("cpu")
         r.status = "done"
         tree.close()
         r.done_at = time.perf_counter() - t_start

@@ -290,6 +290,14 @@ BHUT_API int bhut_tree_import(bhut_tree *t, const double *positions, const doubl
  * FP32-pipe rooflines; no reference counterpart. */
 BHUT_API int bhut_measure_fp32_peak(double *tflops);
 
+/* Bytes in use and reserved by the stream-ordered pool that holds the
+ * engine's device buffers (current device). */
+BHUT_API int bhut_pool_usage(int64_t *used, int64_t *reserved);
+
+/* Returns the pool's reserved but unused device memory to the driver
+ * (synchronises the device); the server calls it after retiring requests. */
+BHUT_API int bhut_pool_trim(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -105,3 +105,12 @@ def test_snapshot_restore_continues_bit_for_bit():
         assert np.array_equal(a.final_positions.cpu().numpy(), b.final_positions.cpu().numpy())
         assert np.array_equal(a.final_velocities.cpu().numpy(),
                               b.final_velocities.cpu().numpy())
+
+
+def test_oversized_request_is_rejected_not_waited_for():
+    reqs = [_req(0, 1500, 7, steps=2), _req(1, 6000, 8, steps=2)]
+    sv = serve.Server(hbm_budget=3000 * serve.bytes_per_particle(16))
+    st = sv.run(reqs, realtime=False, max_seconds=60)
+    sv.close()
+    assert [r.status for r in reqs] == ["done", "rejected"]
+    assert st["requests_done"] == 1 and st["requests_rejected"] == 1
