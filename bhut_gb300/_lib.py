@@ -79,6 +79,8 @@ SIGNATURES = {
     "bhut_batch_configure": (_INT, [_VP, _INT, _INT, _INT, _INT]),
     "bhut_batch_set_multipole": (_INT, [_VP, _INT]),
     "bhut_batch_set_stack": (_INT, [_VP, _INT]),
+    "bhut_batch_roots": (_INT, [_VP, _VP]),
+    "bhut_batch_outside": (_INT, [_VP, _VP, _VP]),
     "bhut_batch_load": (_INT, [_VP, _VP, _VP, _VP, _I64]),
     "bhut_batch_solve": (_INT, [_VP, _D, _D, _D, _VP]),
     "bhut_batch_info": (_INT, [_VP] + [ctypes.POINTER(_I64)] * 4),

@@ -143,6 +143,43 @@ __global__ void k_seg_keep_perm(const int64_t* __restrict__ off, const uint8_t* 
     for (int64_t i = off[s] + threadIdx.x; i < off[s + 1]; i += blockDim.x) perm[i] = perm_in[i];
 }
 
+// should_refit_vs_rebuild (bhut/tree/refit.py:236-249) per system: flag[s]
+// = 1 when a particle of system s lies beyond 1.1 x the root half-size from
+// the root centre (roots: 4 doubles per system, centre and half-size of the
+// root at the system's last rebuild) along some axis.
+__global__ void k_seg_outside(const double* __restrict__ pos, const int64_t* __restrict__ off,
+                              const double* __restrict__ roots, int dim,
+                              uint8_t* __restrict__ flag)
+{
+    const int s = blockIdx.x;
+    const double* r = roots + 4 * s;
+    const double lim = __dmul_rn(1.1, r[3]);
+    bool out = false;
+    for (int64_t i = off[s] + threadIdx.x; i < off[s + 1]; i += blockDim.x) {
+        double mx = fabs(__dsub_rn(pos[i * dim], r[0]));
+        for (int d = 1; d < dim; d++) {
+            const double v = fabs(__dsub_rn(pos[i * dim + d], r[d]));
+            mx = v > mx ? v : mx;
+        }
+        out |= (mx > lim) || !(mx == mx);
+    }
+    out = __syncthreads_or(out);
+    if (threadIdx.x == 0) flag[s] = out ? 1 : 0;
+}
+
+// Root centre and half-size of every system from the last solve.
+__global__ void k_seg_roots(const int64_t* __restrict__ node_off, const double* __restrict__ center,
+                            const double* __restrict__ half, int dim, int64_t ns,
+                            double* __restrict__ roots)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ns;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = node_off[s];
+        for (int d = 0; d < 3; d++) roots[4 * s + d] = d < dim ? center[r * dim + d] : 0.0;
+        roots[4 * s + 3] = half[r];
+    }
+}
+
 // Leapfrog kick and drift: v += kick * a, then x += drift * v.
 __global__ void k_leapfrog(double* __restrict__ pos, double* __restrict__ vel,
                            const double* __restrict__ acc, int64_t n, double kick, double drift)
@@ -1090,6 +1127,47 @@ int bhut_batch_keep_order(bhut_batch* b, const uint8_t* keep, const int32_t* per
                                                       : cudaMemcpyHostToDevice, s));
     if (!b->keep_active) drop_graph(b);
     b->keep_active = true;
+    return kOk;
+}
+
+int bhut_batch_roots(const bhut_batch* b, double* roots)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (!b->layout_valid || !roots) { set_error("nothing to copy"); return kInvalid; }
+    cudaStream_t s = b->stream;
+    BufB tmp;
+    BHUT_TRY(tmp.ensure(sizeof(double) * 4 * b->nsys, s));
+    k_seg_roots<<<grid_for(b->nsys, 128), 128, 0, s>>>(b->d_node_off.as<int64_t>(),
+                                                        b->center.as<double>(),
+                                                        b->half.as<double>(), b->dim, b->nsys,
+                                                        tmp.as<double>());
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
+    BHUT_CUDA(cudaMemcpyAsync(roots, tmp.p, sizeof(double) * 4 * b->nsys, cudaMemcpyDefault, s));
+    BHUT_CUDA(cudaStreamSynchronize(s));
+    tmp.release(s);
+    return kOk;
+}
+
+int bhut_batch_outside(const bhut_batch* b, const double* roots, uint8_t* flags)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (!b->layout_valid || !roots || !flags) { set_error("load systems first"); return kInvalid; }
+    cudaStream_t s = b->stream;
+    BufB droots, dflags;
+    BHUT_TRY(droots.ensure(sizeof(double) * 4 * b->nsys, s));
+    BHUT_TRY(dflags.ensure(b->nsys, s));
+    BHUT_CUDA(cudaMemcpyAsync(droots.p, roots, sizeof(double) * 4 * b->nsys, cudaMemcpyDefault, s));
+    k_seg_outside<<<(unsigned)b->nsys, kSegThreads, 0, s>>>(b->pos.as<double>(),
+                                                           b->d_part_off.as<int64_t>(),
+                                                           droots.as<double>(), b->dim,
+                                                           dflags.as<uint8_t>());
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
+    BHUT_CUDA(cudaMemcpyAsync(flags, dflags.p, b->nsys, cudaMemcpyDefault, s));
+    BHUT_CUDA(cudaStreamSynchronize(s));
+    droots.release(s);
+    dflags.release(s);
     return kOk;
 }
 

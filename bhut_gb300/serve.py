@@ -14,7 +14,9 @@ per tick:
   solve of every resident system (``bhut_batch_*``), second half-kick;
 * each system refits its tree on its own schedule -- its Morton order is kept
   (``bhut_batch_keep_order``) and node boxes and moments are recomputed --
-  and rebuilds it every ``rebuild_every`` of its own steps.  Nothing a system
+  and rebuilds it every ``rebuild_every`` of its own steps, or earlier when a
+  particle leaves 1.1x the root box of its last rebuild (the reference's
+  refit-vs-rebuild test, ``bhut_batch_outside``).  Nothing a system
   computes depends on which other systems share the batch, so a request's
   trajectory is the same alone and in any mix (bit for bit);
 * a finished request leaves at the next tick boundary and frees its slot; so
@@ -116,6 +118,8 @@ class Request:
     admitted_at: float | None = None
     done_at: float | None = None
     order: object = None          # local Morton order of the last solve (device int32)
+    root: object = None           # root centre and half-size at the last rebuild
+    forced_rebuilds: int = 0      # rebuilds forced by particles leaving the root box
     slot: tuple = field(default=(0, 0))
     acc: object = None
 
@@ -240,18 +244,32 @@ class Server:
         keep = np.zeros(len(self.active), dtype=np.uint8)
         perm_in = None
         for k, r in enumerate(self.active):         # refit unless a rebuild is due
-            if keeps_order(r.primed, r.order is not None, r.steps_done, self.rebuild_every):
+            if keeps_order(r.primed, r.order is not None and r.root is not None,
+                           r.steps_done, self.rebuild_every):
                 keep[k] = 1
+        self.solver.load(self.x, self.m, self.off)
+        if keep.any():
+            # and unless a particle left 1.1x the root box of the system's last
+            # rebuild (should_refit_vs_rebuild, bhut/tree/refit.py:236-249)
+            roots = np.zeros((len(self.active), 4))
+            for k, r in enumerate(self.active):
+                if keep[k]:
+                    roots[k] = r.root
+            out = np.zeros(len(self.active), dtype=np.uint8)
+            _lib.check(self.L.bhut_batch_outside(self.solver.h, roots.ctypes.data,
+                                                 out.ctypes.data))
+            for k, r in enumerate(self.active):
+                if keep[k] and out[k]:
+                    keep[k] = 0
+                    r.forced_rebuilds += 1
         if keep.any():
             perm_in = torch.cat([
                 (r.order + int(self.off[k])) if r.order is not None
                 else torch.zeros(r.n, dtype=torch.int32, device="cuda")
                 for k, r in enumerate(self.active)])
-            self.solver.load(self.x, self.m, self.off)
             _lib.check(self.L.bhut_batch_keep_order(self.solver.h, keep.ctypes.data,
                                                     perm_in.data_ptr()))
         else:
-            self.solver.load(self.x, self.m, self.off)
             _lib.check(self.L.bhut_batch_keep_order(self.solver.h, None, None))
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
@@ -260,6 +278,12 @@ class Server:
         ev1.record()
         self._solve_events.append((ev0, ev1))
         _lib.check(self.L.bhut_batch_order(self.solver.h, self.perm.data_ptr()))
+        if not keep.all():                          # root boxes of the rebuilt systems
+            roots = np.zeros((len(self.active), 4))
+            _lib.check(self.L.bhut_batch_roots(self.solver.h, roots.ctypes.data))
+            for k, r in enumerate(self.active):
+                if not keep[k]:
+                    r.root = roots[k].copy()
         for k, r in enumerate(self.active):
             s, e = r.slot
             r.order = self.perm[s:e] - s
@@ -392,7 +416,9 @@ class Server:
                 "deadline": r.deadline, "steps_done": r.steps_done, "solves": r.solves,
                 "primed": r.primed, "admitted_at": r.admitted_at, "resident": r in self.active,
                 "positions": host(r.positions), "velocities": host(r.velocities),
-                "masses": host(r.masses), "acc": host(r.acc), "order": host(r.order)})
+                "masses": host(r.masses), "acc": host(r.acc), "order": host(r.order),
+                "root": None if r.root is None else np.array(r.root, copy=True),
+                "forced_rebuilds": r.forced_rebuilds})
         return {"requests": reqs, "ticks": self.ticks, "solves": self.solves,
                 "accels": self.accels, "cancelled": sorted(self._cancel)}
 
@@ -407,6 +433,7 @@ class Server:
                         steps=d["steps"], kind=d["kind"], deadline=d["deadline"])
             r.steps_done, r.solves, r.primed = d["steps_done"], d["solves"], d["primed"]
             r.admitted_at = d["admitted_at"]
+            r.root, r.forced_rebuilds = d["root"], d["forced_rebuilds"]
             if d["resident"]:
                 r.positions = torch.as_tensor(d["positions"], device="cuda")
                 r.velocities = torch.as_tensor(d["velocities"], device="cuda")

@@ -207,6 +207,15 @@ BHUT_API int bhut_batch_keep_order(bhut_batch *b, const uint8_t *keep, const int
 /* Copies the permutation of the last solve (global indices) to perm. */
 BHUT_API int bhut_batch_order(const bhut_batch *b, int32_t *perm);
 
+/* Root centre (3 doubles, zero-padded in 2-D) and half-size of every system
+ * after the last solve, 4 doubles per system (host or device pointer). */
+BHUT_API int bhut_batch_roots(const bhut_batch *b, double *roots);
+
+/* should_refit_vs_rebuild (bhut/tree/refit.py:236-249) for every system of
+ * the loaded positions against the given roots (4 doubles per system):
+ * flags[s] = 1 when system s must be rebuilt. */
+BHUT_API int bhut_batch_outside(const bhut_batch *b, const double *roots, uint8_t *flags);
+
 BHUT_API void bhut_batch_destroy(bhut_batch *b);
 
 /* Leapfrog update on device arrays (n, dim): v += kick * a, then, when

@@ -114,3 +114,28 @@ def test_oversized_request_is_rejected_not_waited_for():
     sv.close()
     assert [r.status for r in reqs] == ["done", "rejected"]
     assert st["requests_done"] == 1 and st["requests_rejected"] == 1
+
+
+def test_refit_falls_back_to_rebuild_outside_root_box():
+    """A system whose particles leave 1.1x the root box of its last rebuild is
+    rebuilt (the reference's refit-vs-rebuild test), a quiet one is refitted;
+    either way each trajectory is the same alone and in the mix."""
+    def expanding():
+        r = _req(0, 2000, 11, steps=6)
+        r.velocities = 300.0 * r.positions          # +30 % per step of dt = 1e-3
+        return r
+
+    def quiet():
+        return _req(1, 2500, 12, steps=6)
+    alone = expanding()
+    sv = serve.Server(theta=0.5, softening=0.01, dt=1e-3, rebuild_every=100)
+    sv.run([alone], realtime=False)
+    sv.close()
+    mix = [expanding(), quiet()]
+    sv = serve.Server(theta=0.5, softening=0.01, dt=1e-3, rebuild_every=100)
+    sv.run(mix, realtime=False)
+    sv.close()
+    assert alone.forced_rebuilds >= 4 and mix[0].forced_rebuilds == alone.forced_rebuilds
+    assert mix[1].forced_rebuilds == 0
+    assert np.array_equal(mix[0].final_positions.cpu().numpy(),
+                          alone.final_positions.cpu().numpy())
