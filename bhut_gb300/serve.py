@@ -356,7 +356,6 @@ class Server:
             if changed:
                 self._pack()
                 changed = False
-                torch.cuda.empty_cache()   # the pre-pack copies go back to the device
             self.tick()
             torch.cuda.current_stream().synchronize()
             free, total = torch.cuda.mem_get_info()
