@@ -80,6 +80,9 @@ SIGNATURES = {
     "bhut_batch_set_multipole": (_INT, [_VP, _INT]),
     "bhut_batch_set_stack": (_INT, [_VP, _INT]),
     "bhut_batch_roots": (_INT, [_VP, _VP]),
+    "bhut_batch_set_refit_rule": (_INT, [_VP, _INT]),
+    "bhut_batch_set_roots": (_INT, [_VP, _VP]),
+    "bhut_batch_forced": (_INT, [_VP, _VP]),
     "bhut_batch_outside": (_INT, [_VP, _VP, _VP]),
     "bhut_batch_load": (_INT, [_VP, _VP, _VP, _VP, _I64]),
     "bhut_batch_solve": (_INT, [_VP, _D, _D, _D, _VP]),

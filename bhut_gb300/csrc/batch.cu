@@ -167,6 +167,48 @@ __global__ void k_seg_outside(const double* __restrict__ pos, const int64_t* __r
     if (threadIdx.x == 0) flag[s] = out ? 1 : 0;
 }
 
+// The same test on the device inside a solve: a system asked to keep its
+// order (keep[s] = 1) that has a particle beyond 1.1 x its stored root box is
+// rebuilt instead (keep[s] <- 0, forced[s] += 1).
+__global__ void k_seg_keep_outside(const double* __restrict__ pos, const int64_t* __restrict__ off,
+                                   const double* __restrict__ roots, int dim,
+                                   uint8_t* __restrict__ keep, int32_t* __restrict__ forced)
+{
+    const int s = blockIdx.x;
+    if (!keep[s]) return;
+    const double* r = roots + 4 * s;
+    const double lim = __dmul_rn(1.1, r[3]);
+    bool out = false;
+    for (int64_t i = off[s] + threadIdx.x; i < off[s + 1]; i += blockDim.x) {
+        double mx = fabs(__dsub_rn(pos[i * dim], r[0]));
+        for (int d = 1; d < dim; d++) {
+            const double v = fabs(__dsub_rn(pos[i * dim + d], r[d]));
+            mx = v > mx ? v : mx;
+        }
+        out |= (mx > lim) || !(mx == mx);
+    }
+    out = __syncthreads_or(out);
+    if (threadIdx.x == 0 && out) {
+        keep[s] = 0;
+        forced[s] += 1;
+    }
+}
+
+// Root boxes of the systems rebuilt by this solve (keep == NULL: all).
+__global__ void k_seg_roots_update(const int64_t* __restrict__ node_off,
+                                   const double* __restrict__ center,
+                                   const double* __restrict__ half, int dim, int64_t ns,
+                                   const uint8_t* __restrict__ keep, double* __restrict__ roots)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ns;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        if (keep && keep[s]) continue;
+        const int64_t r = node_off[s];
+        for (int d = 0; d < 3; d++) roots[4 * s + d] = d < dim ? center[r * dim + d] : 0.0;
+        roots[4 * s + 3] = half[r];
+    }
+}
+
 // Root centre and half-size of every system from the last solve.
 __global__ void k_seg_roots(const int64_t* __restrict__ node_off, const double* __restrict__ center,
                             const double* __restrict__ half, int dim, int64_t ns,
@@ -693,6 +735,7 @@ struct bhut_batch {
     int dim = 3, leaf = 32, form = BHUT_FORM_FP32, mac = 0, tpw = 32;
     int multipole = BHUT_MULTIPOLE_MONO;
     int stack = BHUT_STACK_SHARED;
+    bool refit_rule = false;        // refit-vs-rebuild test inside the solve
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int64_t nsys = 0, ntot = 0, mtot = 0, ltot = 0;
@@ -702,7 +745,7 @@ struct bhut_batch {
     BufB pos, mass, d_part_off, d_node_off, d_leaf_off, d_tasks, keys, perm, sys_of, key2,
         sx, sy, sz, sm, cm, size, center, half, lo, hi, first_child, start, count, parent,
         leaf_list, arrive, sort_scratch, box, frames, ph, pl, nh, nl, nsize, ndelta, counter,
-        err, stats, out, keep, perm_in, quad, nq0, nq1, nhdr;
+        err, stats, out, keep, perm_in, quad, nq0, nq1, nhdr, roots, forced;
     bool keep_active = false;
     unsigned long long last_stats[5] = {0, 0, 0, 0, 0};
     cudaGraphExec_t graph = nullptr;
@@ -716,7 +759,8 @@ struct bhut_batch {
                         &sys_of, &key2, &sx, &sy, &sz, &sm, &cm, &size, &center, &half, &lo, &hi,
                         &first_child, &start, &count, &parent, &leaf_list, &arrive,
                         &sort_scratch, &box, &frames, &ph, &pl, &nh, &nl, &nsize, &ndelta,
-                        &counter, &err, &stats, &out, &keep, &perm_in, &quad, &nq0, &nq1, &nhdr})
+                        &counter, &err, &stats, &out, &keep, &perm_in, &quad, &nq0, &nq1, &nhdr,
+                        &roots, &forced})
             x->release(stream);
     }
 
@@ -833,6 +877,10 @@ int plan_layout(bhut_batch* b, const int64_t* offsets, int64_t nsys)
     BHUT_TRY(b->stats.ensure(sizeof(unsigned long long) * 8, s));
     BHUT_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(unsigned), s));
     BHUT_TRY(b->keep.ensure(nsys, s));
+    BHUT_TRY(b->roots.ensure(sizeof(double) * 4 * nsys, s));
+    BHUT_TRY(b->forced.ensure(sizeof(int32_t) * nsys, s));
+    BHUT_CUDA(cudaMemsetAsync(b->roots.p, 0, sizeof(double) * 4 * nsys, s));
+    BHUT_CUDA(cudaMemsetAsync(b->forced.p, 0, sizeof(int32_t) * nsys, s));
     BHUT_TRY(b->perm_in.ensure(sizeof(int32_t) * ntot, s));
     b->keep_active = false;
     b->layout_valid = true;
@@ -876,6 +924,13 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
                                   bits_for(ns - 1), b->sort_scratch.p, s));
     }
     if (b->keep_active) {
+        if (b->refit_rule) {
+            k_seg_keep_outside<<<(unsigned)ns, kSegThreads, 0, s>>>(
+                b->pos.as<double>(), b->d_part_off.as<int64_t>(), b->roots.as<double>(), dim,
+                b->keep.as<uint8_t>(), b->forced.as<int32_t>());
+            BHUT_CUDA(cudaGetLastError());
+            note_launches(1);
+        }
         k_seg_keep_perm<<<(unsigned)ns, kSegThreads, 0, s>>>(b->d_part_off.as<int64_t>(),
                                                            b->keep.as<uint8_t>(),
                                                            b->perm_in.as<int32_t>(),
@@ -893,6 +948,13 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
                               b->count.as<int32_t>(), b->parent.as<int32_t>(),
                               b->arrive.as<unsigned>(), o, false, nullptr, nullptr,
                               b->err.as<unsigned>(), s));
+    if (b->refit_rule) {
+        k_seg_roots_update<<<grid_for(ns, 128), 128, 0, s>>>(
+            b->d_node_off.as<int64_t>(), b->center.as<double>(), b->half.as<double>(), dim, ns,
+            b->keep_active ? b->keep.as<uint8_t>() : nullptr, b->roots.as<double>());
+        BHUT_CUDA(cudaGetLastError());
+        note_launches(1);
+    }
     const bool quad = b->form == BHUT_FORM_FP32 && b->multipole == BHUT_MULTIPOLE_QUAD;
     if (quad)
         BHUT_TRY(launch_quadrupoles(b->dev(), b->leaf_list.as<int32_t>(), b->ltot,
@@ -1130,11 +1192,45 @@ int bhut_batch_keep_order(bhut_batch* b, const uint8_t* keep, const int32_t* per
     return kOk;
 }
 
+int bhut_batch_set_refit_rule(bhut_batch* b, int on)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if ((on != 0) != b->refit_rule) drop_graph(b);
+    b->refit_rule = on != 0;
+    return kOk;
+}
+
+int bhut_batch_set_roots(bhut_batch* b, const double* roots)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (!b->layout_valid || !roots) { set_error("load systems first"); return kInvalid; }
+    BHUT_CUDA(cudaMemcpyAsync(b->roots.p, roots, sizeof(double) * 4 * b->nsys, cudaMemcpyDefault,
+                              b->stream));
+    if (!is_device_pointer(roots)) BHUT_CUDA(cudaStreamSynchronize(b->stream));
+    return kOk;
+}
+
+int bhut_batch_forced(const bhut_batch* b, int32_t* counts)
+{
+    if (!b) { set_error("batch is NULL"); return kInvalid; }
+    if (!b->layout_valid || !counts) { set_error("nothing to copy"); return kInvalid; }
+    BHUT_CUDA(cudaMemcpyAsync(counts, b->forced.p, sizeof(int32_t) * b->nsys, cudaMemcpyDefault,
+                              b->stream));
+    BHUT_CUDA(cudaStreamSynchronize(b->stream));
+    return kOk;
+}
+
 int bhut_batch_roots(const bhut_batch* b, double* roots)
 {
     if (!b) { set_error("batch is NULL"); return kInvalid; }
     if (!b->layout_valid || !roots) { set_error("nothing to copy"); return kInvalid; }
     cudaStream_t s = b->stream;
+    if (b->refit_rule) {   // the roots kept by the solves
+        BHUT_CUDA(cudaMemcpyAsync(roots, b->roots.p, sizeof(double) * 4 * b->nsys,
+                                  cudaMemcpyDefault, s));
+        BHUT_CUDA(cudaStreamSynchronize(s));
+        return kOk;
+    }
     BufB tmp;
     BHUT_TRY(tmp.ensure(sizeof(double) * 4 * b->nsys, s));
     k_seg_roots<<<grid_for(b->nsys, 128), 128, 0, s>>>(b->d_node_off.as<int64_t>(),
@@ -1177,7 +1273,7 @@ int bhut_batch_order(const bhut_batch* b, int32_t* perm)
     if (!b->layout_valid || !perm) { set_error("nothing to copy"); return kInvalid; }
     BHUT_CUDA(cudaMemcpyAsync(perm, b->perm.p, sizeof(int32_t) * b->ntot, cudaMemcpyDefault,
                               b->stream));
-    BHUT_CUDA(cudaStreamSynchronize(b->stream));
+    if (!is_device_pointer(perm)) BHUT_CUDA(cudaStreamSynchronize(b->stream));
     return kOk;
 }
 

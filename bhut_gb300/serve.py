@@ -120,6 +120,7 @@ class Request:
     order: object = None          # local Morton order of the last solve (device int32)
     root: object = None           # root centre and half-size at the last rebuild
     forced_rebuilds: int = 0      # rebuilds forced by particles leaving the root box
+    forced_seen: int = 0          # of those, already counted from the solver's counter
     slot: tuple = field(default=(0, 0))
     acc: object = None
 
@@ -179,6 +180,10 @@ class Server:
         self.solver = BatchedSolver(dim=3, leaf_size=leaf_size, form=form, criterion=criterion,
                                     targets_per_warp=targets_per_warp, use_graph=False,
                                     stream=self.stream, multipole=multipole)
+        # the refit-vs-rebuild test runs inside each solve (no host round trip)
+        _lib.check(self.L.bhut_batch_set_refit_rule(self.solver.h, 1))
+        self.packed: list[Request] = []    # systems of the solver's current layout, in order
+        self._roots_dirty = False
         self.active: list[Request] = []
         self.finished: list[Request] = []
         self.ticks = 0
@@ -206,10 +211,27 @@ class Server:
                       leaf_size=self.leaf_size, hbm_budget=self.hbm_budget,
                       max_active=self.max_active)
 
+    def _sync_roots(self) -> None:
+        """Copies the solver's per-system root boxes and forced-rebuild counts
+        of the current layout back into the requests (one host round trip)."""
+        if not self.packed or self._roots_dirty:
+            return
+        ns = len(self.packed)
+        roots = np.zeros((ns, 4))
+        forced = np.zeros(ns, dtype=np.int32)
+        _lib.check(self.L.bhut_batch_roots(self.solver.h, roots.ctypes.data))
+        _lib.check(self.L.bhut_batch_forced(self.solver.h, forced.ctypes.data))
+        for k, r in enumerate(self.packed):
+            if r.primed:
+                r.root = roots[k].copy()
+            r.forced_rebuilds += int(forced[k]) - r.forced_seen
+            r.forced_seen = int(forced[k])
+
     def _pack(self):
         """Concatenates the resident systems' state into one set of device
         arrays (after an admission or a retirement)."""
         torch = self.torch
+        self._sync_roots()
         dev = "cuda"
         parts_x, parts_v, parts_a, parts_m = [], [], [], []
         for r in self.active:
@@ -230,6 +252,8 @@ class Server:
                 self.m[s:e]
             r.slot = (s, e)
         self.perm = torch.empty(int(self.off[-1]), dtype=torch.int32, device=dev)
+        self.packed = list(self.active)
+        self._roots_dirty = True
         self.peak_bytes = max(self.peak_bytes,
                               float(self.off[-1]) * bytes_per_particle(self.leaf_size))
 
@@ -244,24 +268,21 @@ class Server:
         keep = np.zeros(len(self.active), dtype=np.uint8)
         perm_in = None
         for k, r in enumerate(self.active):         # refit unless a rebuild is due
-            if keeps_order(r.primed, r.order is not None and r.root is not None,
-                           r.steps_done, self.rebuild_every):
+            if keeps_order(r.primed, r.order is not None, r.steps_done, self.rebuild_every):
                 keep[k] = 1
         self.solver.load(self.x, self.m, self.off)
-        if keep.any():
-            # and unless a particle left 1.1x the root box of the system's last
-            # rebuild (should_refit_vs_rebuild, bhut/tree/refit.py:236-249)
+        if self._roots_dirty:
+            # a new layout: its systems' root boxes (those never rebuilt are
+            # not kept anyway), forced-rebuild counters from zero.  Inside the
+            # solve a kept system that has a particle beyond 1.1x its root box
+            # is rebuilt (should_refit_vs_rebuild, bhut/tree/refit.py:236-249).
             roots = np.zeros((len(self.active), 4))
             for k, r in enumerate(self.active):
-                if keep[k]:
+                if r.root is not None:
                     roots[k] = r.root
-            out = np.zeros(len(self.active), dtype=np.uint8)
-            _lib.check(self.L.bhut_batch_outside(self.solver.h, roots.ctypes.data,
-                                                 out.ctypes.data))
-            for k, r in enumerate(self.active):
-                if keep[k] and out[k]:
-                    keep[k] = 0
-                    r.forced_rebuilds += 1
+                r.forced_seen = 0
+            _lib.check(self.L.bhut_batch_set_roots(self.solver.h, roots.ctypes.data))
+            self._roots_dirty = False
         if keep.any():
             perm_in = torch.cat([
                 (r.order + int(self.off[k])) if r.order is not None
@@ -278,12 +299,6 @@ class Server:
         ev1.record()
         self._solve_events.append((ev0, ev1))
         _lib.check(self.L.bhut_batch_order(self.solver.h, self.perm.data_ptr()))
-        if not keep.all():                          # root boxes of the rebuilt systems
-            roots = np.zeros((len(self.active), 4))
-            _lib.check(self.L.bhut_batch_roots(self.solver.h, roots.ctypes.data))
-            for k, r in enumerate(self.active):
-                if not keep[k]:
-                    r.root = roots[k].copy()
         for k, r in enumerate(self.active):
             s, e = r.slot
             r.order = self.perm[s:e] - s
@@ -324,6 +339,7 @@ class Server:
             return time.perf_counter() - t_start
 
         changed = bool(self.active)
+        inflight = []
         while queue or self.active:
             t = now()
             if max_seconds is not None and t > max_seconds:
@@ -357,7 +373,13 @@ class Server:
                 self._pack()
                 changed = False
             self.tick()
-            torch.cuda.current_stream().synchronize()
+            # the host runs at most two ticks ahead of the GPU: the next tick
+            # is prepared while this one computes
+            ev = torch.cuda.Event()
+            ev.record()
+            inflight.append(ev)
+            if len(inflight) > 2:
+                inflight.pop(0).synchronize()
             free, total = torch.cuda.mem_get_info()
             self.mem_peak = max(self.mem_peak, total - free)
 
@@ -368,6 +390,9 @@ class Server:
                                     r.rid in self._cancel)
                 if why:
                     leaving.append((r, why))
+            if leaving:
+                self._sync_roots()        # waits for the GPU; credits forced rebuilds
+                t = now()
             for r, why in leaving:
                 self.active.remove(r)
                 self._leave(r, why, t)
@@ -378,8 +403,9 @@ class Server:
                     changed = False
                 torch.cuda.empty_cache()  # and hand their blocks back
                 _lib.check(self.L.bhut_pool_trim())
-        wall = now() - t0
         torch.cuda.synchronize()
+        wall = now() - t0
+        self._sync_roots()
         solve_s = sum(a.elapsed_time(b) for a, b in self._solve_events) / 1e3
         self._solve_events = []
         done = [r for r in self.finished if r.status == "done"]
@@ -405,6 +431,8 @@ class Server:
     def snapshot(self) -> dict:
         """Host copy of every queued and resident request's state (call
         between ticks, e.g. after ``run(max_ticks=k)``)."""
+        self.torch.cuda.synchronize()
+        self._sync_roots()
         def host(x):
             return None if x is None else (x.cpu().numpy().copy() if hasattr(x, "cpu")
                                            else np.array(x, copy=True))

@@ -204,11 +204,22 @@ BHUT_API int bhut_batch_stats(const bhut_batch *b, int64_t *p2p, int64_t *m2p, i
  * is unchanged.  keep == NULL returns to a full rebuild of every system. */
 BHUT_API int bhut_batch_keep_order(bhut_batch *b, const uint8_t *keep, const int32_t *perm);
 
-/* Copies the permutation of the last solve (global indices) to perm. */
+/* Copies the permutation of the last solve (global indices) to perm; stream
+ * ordered (no host synchronisation) when perm is device memory. */
 BHUT_API int bhut_batch_order(const bhut_batch *b, int32_t *perm);
 
-/* Root centre (3 doubles, zero-padded in 2-D) and half-size of every system
- * after the last solve, 4 doubles per system (host or device pointer). */
+/* The refit-vs-rebuild test inside the solve (on: 1): a system asked to keep
+ * its order (bhut_batch_keep_order) is rebuilt instead when a particle lies
+ * beyond 1.1 x its stored root box (bhut/tree/refit.py:236-249); every
+ * rebuilt system's root box is stored.  Roots and counts of forced rebuilds
+ * are per system of the current layout (zeroed by a new layout). */
+BHUT_API int bhut_batch_set_refit_rule(bhut_batch *b, int on);
+BHUT_API int bhut_batch_set_roots(bhut_batch *b, const double *roots);
+BHUT_API int bhut_batch_forced(const bhut_batch *b, int32_t *counts);
+
+/* Root centre (3 doubles, zero-padded in 2-D) and half-size of every system,
+ * 4 doubles per system (host or device pointer): the stored roots with the
+ * refit rule on, else those of the last solve. */
 BHUT_API int bhut_batch_roots(const bhut_batch *b, double *roots);
 
 /* should_refit_vs_rebuild (bhut/tree/refit.py:236-249) for every system of
