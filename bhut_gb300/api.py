@@ -543,11 +543,18 @@ class Tree:
         new_positions, new_masses, _ = _validate_accelerations_inputs(
             new_positions, new_masses, dim=self.dim, softening=0.0, theta=0.5, G=1.0,
             leaf_size=self.leaf_size)
+        if _shape(new_positions)[0] == 0:
+            raise ValueError("Cannot build tree with zero particles")
+        if self._handle is None:
+            self._handle = _Handle(self.dim, self.leaf_size)
+        # the device rejects non-finite input before touching the built tree,
+        # so a failed rebuild leaves this Tree as it was
+        self._handle.build(new_positions, new_masses)
         self.positions = new_positions
         self.masses = new_masses
-        self._is_built = False
         self._tree_cache = None
-        return self.build()
+        self._is_built = True
+        return self
 
     def accelerations(self, targets=None, *, theta: float = 0.5, softening: Any = 0.0,
                       G: float = 1.0):

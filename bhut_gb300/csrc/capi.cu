@@ -6,6 +6,7 @@
 #include <cstring>
 #include <string>
 
+#include <utility>
 #include "../../include/bhut_gb300.h"
 #include "tree.cuh"
 
@@ -104,6 +105,7 @@ struct bhut_tree {
     bool topo_valid = false;
     // particles
     DevBuf pos, mass, keys, perm, sx, sy, sz, sm;
+    DevBuf pos_in, mass_in;   // new inputs, checked before they replace pos / mass
     // nodes
     DevBuf cm, size, center, half, lo, hi, first_child, start, count, parent, leaf_list, arrive;
     // scratch
@@ -239,13 +241,26 @@ int load_particles(bhut_tree* t, const double* positions, const double* masses, 
         return kInvalid;
     }
     if (!positions) { set_error("positions is NULL"); return kInvalid; }
-    BHUT_TRY(stage_in(t->pos, positions, sizeof(double) * n * t->dim, t->stream));
-    if (masses) {
-        BHUT_TRY(stage_in(t->mass, masses, sizeof(double) * n, t->stream));
-    } else if (n != t->n || !t->mass.p) {
+    if (!masses && (n != t->n || !t->mass.p)) {
         set_error("masses are required when the particle count changes");
         return kInvalid;
     }
+    // stage and check first: a rejected input leaves the built tree intact
+    cudaStream_t s = t->stream;
+    BHUT_TRY(stage_in(t->pos_in, positions, sizeof(double) * n * t->dim, s));
+    if (masses) BHUT_TRY(stage_in(t->mass_in, masses, sizeof(double) * n, s));
+    unsigned* flag = t->counters.as<unsigned>() + 4;
+    BHUT_TRY(launch_check_finite(t->pos_in.as<double>(), n * t->dim,
+                                 masses ? t->mass_in.as<double>() : nullptr, n, flag, s));
+    unsigned bad = 0;
+    BHUT_CUDA(cudaMemcpyAsync(&bad, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    BHUT_CUDA(cudaStreamSynchronize(s));
+    if (bad) {
+        set_error("positions must be finite (NaN or Inf found)");
+        return kInvalid;
+    }
+    std::swap(t->pos, t->pos_in);
+    if (masses) std::swap(t->mass, t->mass_in);
     return kOk;
 }
 
@@ -421,8 +436,8 @@ int bhut_tree_build(bhut_tree* t, const double* positions, const double* masses,
 {
     if (!t) { set_error("tree is NULL"); return kInvalid; }
     if (!masses) { set_error("masses is NULL"); return kInvalid; }
+    BHUT_TRY(load_particles(t, positions, masses, n));   // rejected input: tree unchanged
     t->built = false;
-    BHUT_TRY(load_particles(t, positions, masses, n));
     return do_build(t, n);
 }
 
@@ -662,7 +677,7 @@ void bhut_tree_destroy(bhut_tree* t)
                      &t->sort_scratch, &t->box_partial, &t->box, &t->counters, &t->err, &t->stats,
                      &t->tpos, &t->tkeys, &t->tperm, &t->tx, &t->ty, &t->tz, &t->tbox, &t->out,
                      &t->frame, &t->ph, &t->pl, &t->nh, &t->nl, &t->nsize, &t->ndelta, &t->th,
-                     &t->tl, &t->quad, &t->nq0, &t->nq1, &t->nhdr};
+                     &t->tl, &t->quad, &t->nq0, &t->nq1, &t->nhdr, &t->pos_in, &t->mass_in};
     for (DevBuf* b : all) b->release(s);
     cudaStreamSynchronize(s);
     if (t->own_stream) cudaStreamDestroy(s);

@@ -199,6 +199,8 @@ int launch_import_perm(const int64_t* in, int64_t n, int32_t* out, unsigned* err
 int launch_iota(int32_t* out, int64_t n, cudaStream_t s);
 int launch_widen_i32(const int32_t* in, int64_t n, int64_t* out, cudaStream_t s);
 int measure_fp32_peak(double* tflops);
+int launch_check_finite(const double* a, int64_t n, const double* b, int64_t m, unsigned* flag,
+                        cudaStream_t s);
 
 int direct_chunks(int64_t n, int64_t nt);
 int launch_direct(const double* pos, const double* mass, int64_t n, int dim, const double* targets,

@@ -141,3 +141,50 @@ def test_two_body_extremes(form, oracle_mod):
         assert np.all(np.isfinite(acc))
         assert np.allclose(acc, ref, rtol=tol, atol=0.0), (form, pos, acc, ref)
         assert np.allclose(acc[0], -acc[1] * m[1] / m[0], rtol=1e-12 if form != "fp32" else 1e-6)
+
+
+def test_rejected_refit_leaves_tree_intact():
+    """A refit with non-finite positions raises and the built tree still
+    gives its previous accelerations (tests/integration/test_workflows.py:262-280
+    in the reference checks the same for an invalid update)."""
+    pos, m = workloads.gaussian(3000, seed=14)
+    t = bh.Tree(pos, m, leaf_size=16).build()
+    a0 = t.accelerations(theta=0.5, softening=0.01)
+    bad = pos.copy()
+    bad[17, 1] = np.nan
+    with pytest.raises(ValueError, match="finite"):
+        t.refit(bad)
+    with pytest.raises(ValueError, match="finite"):
+        t.rebuild(np.where(np.isnan(bad), np.inf, bad))
+    a1 = t.accelerations(theta=0.5, softening=0.01)
+    assert np.array_equal(a0, a1)
+    t.close()
+
+
+@pytest.mark.parametrize("form", ["exact", "fast"])
+def test_physics_invariants(form):
+    """Known answers and invariants of the reference's physics tests:
+    regular tetrahedron (equal magnitudes, pointing at the centroid), inverse
+    square, momentum sum, theta -> 0 against the direct sum, float32 inputs."""
+    tet = np.array([[1.0, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]])
+    a = bh.accelerations(tet, np.ones(4), theta=0.0, form=form)
+    mags = np.linalg.norm(a, axis=1)
+    assert np.allclose(mags, mags[0], rtol=1e-12)
+    unit_in = -tet / np.linalg.norm(tet, axis=1)[:, None]
+    assert np.allclose(a / mags[:, None], unit_in, rtol=0, atol=1e-12)
+    d1 = bh.accelerations(np.array([[0.0, 0, 0], [2.0, 0, 0]]), np.ones(2), form=form)
+    d2 = bh.accelerations(np.array([[0.0, 0, 0], [4.0, 0, 0]]), np.ones(2), form=form)
+    assert np.isclose(d1[0, 0] / d2[0, 0], 4.0, rtol=1e-12)
+    pos, m = workloads.gaussian(500, seed=15)
+    m = np.random.default_rng(1).uniform(0.5, 2.0, 500)
+    a0 = bh.accelerations(pos, m, theta=0.0, softening=0.01, form=form)
+    assert np.abs((m[:, None] * a0).sum(0)).max() < 1e-12 * np.abs(m[:, None] * a0).sum()
+    direct = np.asarray(bh.direct_accelerations(pos, m, softening=0.01))
+    a8 = bh.accelerations(pos, m, theta=1e-8, softening=0.01, form=form)
+    assert rel_l2(a8, direct) < (1e-12 if form == "exact" else 1e-11)
+    a32 = bh.accelerations(pos.astype(np.float32), m.astype(np.float32), theta=0.5,
+                           softening=0.01, form=form)
+    a64 = bh.accelerations(pos.astype(np.float32).astype(np.float64),
+                           m.astype(np.float32).astype(np.float64), theta=0.5, softening=0.01,
+                           form=form)
+    assert np.array_equal(a32, a64) and a32.dtype == np.float64
