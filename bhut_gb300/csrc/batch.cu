@@ -338,7 +338,7 @@ k_seg_frames(TreeDev t, const int64_t* __restrict__ part_off, const int64_t* __r
     }
     for (int64_t k = node_off[s] + threadIdx.x; k < node_off[s + 1]; k += blockDim.x) {
         const NodeCM c = t.cm[k];
-        nhdr[k] = make_int4(t.first_child[k], t.start[k], t.count[k], c.w != 0.0);
+
         float4 h, l;
         split_grid(__dmul_rn(__dsub_rn(c.x, f.c[0]), f.s), h.x, l.x);
         split_grid(__dmul_rn(__dsub_rn(c.y, f.c[1]), f.s), h.y, l.y);
@@ -355,6 +355,12 @@ k_seg_frames(TreeDev t, const int64_t* __restrict__ part_off, const int64_t* __r
             dd += v * v;
         }
         ndelta[k] = __double2float_ru(sqrt(dd) * f.s);
+        // header: leaf (-1, start, count, mass != 0); internal (first child,
+        // size, |com - centre| as float bits, mass != 0)
+        const int fc = t.first_child[k];
+        nhdr[k] = fc < 0 ? make_int4(fc, t.start[k], t.count[k], c.w != 0.0)
+                         : make_int4(fc, __float_as_int(nsize[k]), __float_as_int(ndelta[k]),
+                                     c.w != 0.0);
         if (quad) {   // mass x length^2: scale by ms s^2
             const double qs = f.ms * f.s * f.s;
             const double* q = quad + 6 * k;
@@ -589,9 +595,9 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                         d2 = fmaf(d, d, d2);
                     }
                     const float dist = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
-                    const float size_f = b.nsize[node];
+                    const float size_f = __int_as_float(hd.y);
                     if (FP32) {
-                        open = a.mac == 1 ? size_f >= theta_f * (dist - b.ndelta[node])
+                        open = a.mac == 1 ? size_f >= theta_f * (dist - __int_as_float(hd.z))
                                           : (dist == 0.0f || size_f >= theta_f * dist);
                     } else {
                         const float td = theta_f * dist;

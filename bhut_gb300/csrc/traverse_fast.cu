@@ -91,7 +91,7 @@ __global__ void k_ff_nodes(TreeDev t, const double* __restrict__ center,
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < t.m;
          k += (int64_t)gridDim.x * blockDim.x) {
         NodeCM c = t.cm[k];
-        nhdr[k] = make_int4(t.first_child[k], t.start[k], t.count[k], c.w != 0.0);
+
         float4 h, l;
         // a node's COM lies inside the box: |u| <= 1 up to rounding
         split_grid(__dmul_rn(__dsub_rn(c.x, f.c[0]), f.s), h.x, l.x);
@@ -110,6 +110,12 @@ __global__ void k_ff_nodes(TreeDev t, const double* __restrict__ center,
             dd += v * v;
         }
         ndelta[k] = __double2float_ru(sqrt(dd) * f.s);
+        // header: leaf (-1, start, count, mass != 0); internal (first child,
+        // size, |com - centre| as float bits, mass != 0)
+        const int fc = t.first_child[k];
+        nhdr[k] = fc < 0 ? make_int4(fc, t.start[k], t.count[k], c.w != 0.0)
+                         : make_int4(fc, __float_as_int(nsize[k]), __float_as_int(ndelta[k]),
+                                     c.w != 0.0);
         if (quad) {   // mass x length^2: scale by ms s^2
             const double qs = f.ms * f.s * f.s;
             const double* q = quad + 6 * k;
@@ -245,7 +251,7 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                 const float dist = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
                 const float td = theta_f * dist;
                 const float band = theta_f * fmaf(kBandRel, dist, band_abs);
-                const float size_f = ft.nsize[node];
+                const float size_f = __int_as_float(hd.y);
                 if (size_f >= td + band) {
                     open = true;
                 } else if (size_f < td - band) {
@@ -408,10 +414,10 @@ __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, c
                     d2 = fmaf(d, d, d2);
                 }
                 const float dist = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
-                const float size_f = ft.nsize[node];
+                const float size_f = __int_as_float(hd.y);
                 if (a.mac == 1) {
                     // offset criterion: open when d < size/theta + |com - centre|
-                    open = size_f >= theta_f * (dist - ft.ndelta[node]);
+                    open = size_f >= theta_f * (dist - __int_as_float(hd.z));
                 } else {
                     open = dist == 0.0f || size_f >= theta_f * dist;
                 }

@@ -70,7 +70,8 @@ struct FastTree {
     const float* ndelta; // |com - AABB centre|, normalised, per node (offset criterion)
     const float4* nq0;   // quadrupole (xx, yy, zz, xy), normalised, per node; NULL: monopoles
     const float2* nq1;   // quadrupole (xz, yz)
-    const int4* nhdr;    // (first_child, start, count, mass != 0) per node: one load per visit
+    const int4* nhdr;    // per node, one load per visit: leaf (-1, start, count, mass != 0),
+                         // internal (first child, size, |com - centre| as float bits, mass != 0)
 };
 
 // Morton encoding (bhut/utils/morton.py:14-45, 183-198) and the quantisation
