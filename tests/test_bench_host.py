@@ -53,3 +53,29 @@ def test_reference_arm_two_ranks():
     assert d["impl"] == "reference" and d["unit"] == "accels/s" and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_clock_sampler_parsing():
+    """Median SM clock, max clock and active throttle reasons from the
+    nvidia-smi CSV lines sampled during the timed region."""
+    sys.path.insert(0, REPO)
+    import bench
+    cs = bench.ClockSampler(0)
+    cs.proc = type("P", (), {"terminate": lambda self: None, "wait": lambda self, timeout=None: 0})()
+    cs.lines = ["0, 2070, 2070, 900.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+                "0, 2040, 2070, 1300.0, 0x4, Not Active, Not Active, Not Active, Active",
+                "0, 2070, 2070, 1350.0, 0x4, Not Active, Not Active, Not Active, Active",
+                "garbage"]
+    got = cs.stop()
+    assert got["sm_mhz"] == 2070.0 and got["sm_max_mhz"] == 2070.0
+    assert got["reasons"] == ["sw_power_cap"] and got["samples"] == 3
+
+
+def test_workload_description_and_threads():
+    sys.path.insert(0, REPO)
+    import bench
+    d = bench._workload_desc(1_000_000, "fast")
+    assert d["workload"].startswith("Plummer sphere N=1,000,000")
+    assert d["theta"] == 0.5 and d["softening"] == 0.01 and d["leaf_size"] == 32
+    assert "L2 flush" in d["l2"] or "flush" in d["l2"]
+    assert bench.host_threads() >= 1
