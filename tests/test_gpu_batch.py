@@ -108,3 +108,33 @@ def test_stack_placements_agree(systems, form, tpw):
     assert res["shared"][1] == res["registers"][1]
     with pytest.raises(ValueError, match="stack must be"):
         batch.BatchedSolver(stack="global")
+
+
+def test_batch_roots_and_outside_test():
+    """The per-system refit-vs-rebuild test as a call: roots of the last
+    solve, then flags for positions moved beyond 1.1x a root box."""
+    import ctypes
+    from bhut_gb300 import _lib
+    L = _lib.load()
+    systems = workloads.plummer_batch(nsys=3, nmin=500, nmax=2000, seed=9)
+    pos, m, off = batch.concat_systems(systems)
+    sv = batch.BatchedSolver(form="fp32", use_graph=False)
+    sv.load(pos, m, off)
+    sv.solve(theta=0.5, softening=0.01)
+    roots = np.zeros((3, 4))
+    _lib.check(L.bhut_batch_roots(sv.h, roots.ctypes.data))
+    for s, (p, _) in enumerate(systems):
+        lo, hi = p.min(0), p.max(0)
+        assert np.all(roots[s, :3] >= lo) and np.all(roots[s, :3] <= hi)
+        assert roots[s, 3] >= 0.5 * (hi - lo).max() * (1 - 1e-12)
+    moved = pos.copy()
+    moved[off[1]:off[2]] *= 3.0
+    sv.load(moved, m, off)
+    flags = np.zeros(3, dtype=np.uint8)
+    _lib.check(L.bhut_batch_outside(sv.h, roots.ctypes.data, flags.ctypes.data))
+    assert flags.tolist() == [0, 1, 0]
+    used, reserved = ctypes.c_int64(), ctypes.c_int64()
+    _lib.check(L.bhut_pool_usage(ctypes.byref(used), ctypes.byref(reserved)))
+    assert used.value > 0 and reserved.value >= used.value
+    sv.close()
+    _lib.check(L.bhut_pool_trim())
