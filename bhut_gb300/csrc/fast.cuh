@@ -92,7 +92,12 @@ static __device__ __forceinline__ float comp(const float4& v, int k)
 // |gl| <= ulp(gh) / 2; every later product of a float-float with g then
 // keeps ~2^-47 relative accuracy.  A pair at zero displacement (the target
 // itself, or a duplicate) contributes exactly zero, as in the reference.
-template <int DIM, bool FAR>
+//
+// CHECK = false: the caller guarantees R >= kTinyR for every pair (a target
+// inside the box and a softening with (eps s)^2 >= 2 kTinyR: R >= eps^2 up to
+// the 2^-20 relative error of the error terms), so the test and its selects
+// are compiled out and the result is the same bit for bit.
+template <int DIM, bool FAR, bool CHECK = true>
 __device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4 sh, float4 sl,
                                         float e2h, float e2l, float* ah, float* al)
 {
@@ -127,7 +132,7 @@ __device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4
     }
     const float Rs = __fadd_rn(s, lo);
     // |dx| <= 2 inside the box: only FAR targets can exceed kHugeR
-    const bool ok = FAR ? (Rs >= kTinyR && Rs <= kHugeR) : (Rs >= kTinyR);
+    const bool ok = FAR ? (Rs >= kTinyR && Rs <= kHugeR) : (!CHECK || Rs >= kTinyR);
     const float Rh = ok ? Rs : 1.0f;
     const float Rl = ok ? __fsub_rn(lo, __fsub_rn(Rs, s)) : 0.0f;
     // w = R^(-3/2): y ~ R^(-1/2); e = 1 - R y^2 exactly enough;

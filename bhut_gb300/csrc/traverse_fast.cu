@@ -171,7 +171,7 @@ struct FastArgs {
     int mac;                 // 0: reference criterion, 1: offset criterion (fp32 form)
 };
 
-template <int DIM, bool FAR>
+template <int DIM, bool FAR, bool CHECK>
 __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const FastArgs& a,
                                      int w, int lane, bool valid, int64_t me_sorted, const float* Th,
                                      const float* Tl, float band_abs, double x, double y, double z,
@@ -215,8 +215,8 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                     unsigned fb = 0;   // pairs left to FP64 (rare), taken after the loop
 #pragma unroll (kFFUnroll)
                     for (int q = 0; q < cn; q++)
-                        fb |= (unsigned)!pair_ff<DIM, FAR>(Th, Tl, sh[w][q], sl[w][q], a.e2h,
-                                                           a.e2l, ah, al) << q;
+                        fb |= (unsigned)!pair_ff<DIM, FAR, CHECK>(Th, Tl, sh[w][q], sl[w][q],
+                                                                  a.e2h, a.e2l, ah, al) << q;
                     while (fb) {
                         const int gi = s + b + __ffs(fb) - 1;
                         fb &= fb - 1;
@@ -264,7 +264,7 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
             const unsigned omask = __ballot_sync(FULL, act && open);
             if (act && !open) {
                 const float4 nl = ft.nl[node];   // (cached: read by the opening test)
-                if (!pair_ff<DIM, FAR>(Th, Tl, nh, nl, a.e2h, a.e2l, ah, al)) {
+                if (!pair_ff<DIM, FAR, CHECK>(Th, Tl, nh, nl, a.e2h, a.e2l, ah, al)) {
                     const NodeCM cm = t.cm[node];
                     pair_fp64<DIM>(x, y, z, cm.x, cm.y, cm.z, cm.w, eps2, a64);
                     cnt[4]++;
@@ -284,7 +284,9 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
     }
 }
 
-template <int DIM>
+// SOFT: (eps s)^2 >= 2 kTinyR, so a warp of targets inside the box needs no
+// small-R test (pair_ff's CHECK).
+template <int DIM, bool SOFT>
 __global__ void __launch_bounds__(kFastThreads, kFastBlocksPerSM)
 k_traverse_fast(TreeDev t, FastTree ft, FastArgs a)
 {
@@ -323,11 +325,11 @@ k_traverse_fast(TreeDev t, FastTree ft, FastArgs a)
         const int64_t me_sorted = (valid && a.th == nullptr) ? i : -1;
         bool overflow = false;
         if (__any_sync(FULL, far))
-            walk<DIM, true>(t, ft, a, w, lane, valid, me_sorted, Th, Tl, band_abs, x, y, z, ah, al,
-                            a64, stack, sh, sl, cnt, overflow);
+            walk<DIM, true, true>(t, ft, a, w, lane, valid, me_sorted, Th, Tl, band_abs, x, y, z,
+                                  ah, al, a64, stack, sh, sl, cnt, overflow);
         else
-            walk<DIM, false>(t, ft, a, w, lane, valid, me_sorted, Th, Tl, band_abs, x, y, z, ah, al,
-                             a64, stack, sh, sl, cnt, overflow);
+            walk<DIM, false, !SOFT>(t, ft, a, w, lane, valid, me_sorted, Th, Tl, band_abs, x, y, z,
+                                    ah, al, a64, stack, sh, sl, cnt, overflow);
         if (overflow && lane == 0) atomicOr(a.err, kErrStackOverflow);
         if (a.stats) {
 #pragma unroll
@@ -534,10 +536,15 @@ int launch_traverse_fast(const TreeDev& t, const FastTree& ft, const float4* th,
     if (fp32) {
         if (t.dim == 3) k_traverse_fp32<3><<<grid, kFastThreads, 0, s>>>(t, ft, a);
         else k_traverse_fp32<2><<<grid, kFastThreads, 0, s>>>(t, ft, a);
-    } else if (t.dim == 3) {
-        k_traverse_fast<3><<<grid, kFastThreads, 0, s>>>(t, ft, a);
     } else {
-        k_traverse_fast<2><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+        const bool soft = a.e2h >= 2.0f * kTinyR;
+        if (t.dim == 3) {
+            if (soft) k_traverse_fast<3, true><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+            else k_traverse_fast<3, false><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+        } else {
+            if (soft) k_traverse_fast<2, true><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+            else k_traverse_fast<2, false><<<grid, kFastThreads, 0, s>>>(t, ft, a);
+        }
     }
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
