@@ -507,6 +507,8 @@ k_batch_traverse(BatchDev b, BatchArgs a)
         const double e2 = __dmul_rn(es, es);
         const float e2h = __double2float_rn(e2);
         const float e2l = __double2float_rn(__dsub_rn(e2, (double)e2h));
+        // softening large enough that no pair needs the small-R test
+        const bool soft = FP32 ? e2h >= 0x1p-126f : e2h >= 2.0f * kTinyR;
 
         float Th[3] = {0.f, 0.f, 0.f}, Tl[3] = {0.f, 0.f, 0.f};
         double x = 0.0, y = 0.0, z = 0.0;
@@ -550,15 +552,30 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                         if (sub == 0) cnt[0] += cn - (i >= s0 + bb && i < s0 + bb + cn);
                         if (FP32) {   // <= 32 terms in FP32, then one Kahan step
                             float part[3] = {0.f, 0.f, 0.f};
+                            if (soft) {
 #pragma unroll 8
-                            for (int q = sub; q < cn; q += LPT)
-                                pair_f32_partial<DIM>(Th, Tl, sh[w][q], sl[w][q], e2h, part);
+                                for (int q = sub; q < cn; q += LPT)
+                                    pair_f32_partial<DIM, false>(Th, Tl, sh[w][q], sl[w][q], e2h,
+                                                                 part);
+                            } else {
+#pragma unroll 8
+                                for (int q = sub; q < cn; q += LPT)
+                                    pair_f32_partial<DIM, true>(Th, Tl, sh[w][q], sl[w][q], e2h,
+                                                                part);
+                            }
                             kahan_add_f32<DIM>(part, ah, al);
                         } else {
                             unsigned fb = 0;   // pairs left to FP64, taken after the loop
-                            for (int q = sub; q < cn; q += LPT)
-                                fb |= (unsigned)!pair_ff<DIM, false>(Th, Tl, sh[w][q], sl[w][q],
-                                                                     e2h, e2l, ah, al) << q;
+                            if (soft) {
+                                for (int q = sub; q < cn; q += LPT)
+                                    pair_ff<DIM, false, false>(Th, Tl, sh[w][q], sl[w][q], e2h,
+                                                               e2l, ah, al);
+                            } else {
+                                for (int q = sub; q < cn; q += LPT)
+                                    fb |= (unsigned)!pair_ff<DIM, false>(Th, Tl, sh[w][q],
+                                                                         sl[w][q], e2h, e2l, ah,
+                                                                         al) << q;
+                            }
                             while (fb) {
                                 const int gi = s0 + bb + __ffs(fb) - 1;
                                 fb &= fb - 1;

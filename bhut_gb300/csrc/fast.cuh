@@ -233,7 +233,10 @@ __device__ __forceinline__ void pair_f32(const float* Th, const float* Tl, float
 // leaf loop sums at most 32 such terms and then adds the partial to the
 // Kahan-compensated per-target accumulator with kahan_add_f32 (blocked
 // Kahan summation).  Same displacement, r^2 and force as pair_f32.
-template <int DIM>
+// CHECK = false: the caller guarantees e2 >= 2^-126; r^2 is an FMA chain of
+// non-negative terms started at e2, so r^2 >= e2 and the test is compiled out
+// (same result bit for bit).
+template <int DIM, bool CHECK = true>
 __device__ __forceinline__ void pair_f32_partial(const float* Th, const float* Tl, float4 sh,
                                                  float4 sl, float e2, float* p)
 {
@@ -242,7 +245,7 @@ __device__ __forceinline__ void pair_f32_partial(const float* Th, const float* T
     const float d2 = DIM == 3 ? __fadd_rn(__fsub_rn(sh.z, Th[2]), __fsub_rn(sl.z, Tl[2])) : 0.0f;
     float r2 = fmaf(d1, d1, fmaf(d0, d0, e2));
     if (DIM == 3) r2 = fmaf(d2, d2, r2);
-    const bool ok = r2 >= 0x1p-126f;
+    const bool ok = !CHECK || r2 >= 0x1p-126f;
     const float ri = rsqrt_mufu(ok ? r2 : 1.0f);
     const float f = ok ? sh.w * (ri * ri * ri) : 0.0f;
     p[0] = fmaf(f, d0, p[0]);

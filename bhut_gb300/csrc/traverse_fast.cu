@@ -367,6 +367,7 @@ __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, c
 {
     const unsigned FULL = 0xffffffffu;
     const float theta_f = (float)a.theta;
+    const bool soft = a.e2h >= 0x1p-126f;   // r^2 >= eps^2 is normal: no small-r test
     const unsigned live = __ballot_sync(FULL, valid);
     if (lane == 0) stack[w][0] = make_int2(0, (int)live);
     int sp = 1;
@@ -394,9 +395,15 @@ __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, c
                 if (act) {
                     cnt[0] += cn - (me_sorted >= s + b && me_sorted < s + b + cn);
                     float part[3] = {0.f, 0.f, 0.f};   // <= 32 terms, then one Kahan step
+                    if (soft) {
 #pragma unroll (kF32Unroll)
-                    for (int q = 0; q < cn; q++)
-                        pair_f32_partial<DIM>(T, Tl, sh[w][q], sl[w][q], a.e2h, part);
+                        for (int q = 0; q < cn; q++)
+                            pair_f32_partial<DIM, false>(T, Tl, sh[w][q], sl[w][q], a.e2h, part);
+                    } else {
+#pragma unroll (kF32Unroll)
+                        for (int q = 0; q < cn; q++)
+                            pair_f32_partial<DIM, true>(T, Tl, sh[w][q], sl[w][q], a.e2h, part);
+                    }
                     kahan_add_f32<DIM>(part, acc, cmp);
                 }
                 __syncwarp();
