@@ -216,6 +216,15 @@ def served_report(count: int = 24, rate: float = 200.0, steps: int = 100, seed: 
                                     softening=0.01, form="fast")
             errs_eq.append(precision.error_distribution(a_q[idx], ref)["median"])
     _log(f"median errors: served {errs_srv}, plain {errs_plain}")
+    # warm-up: two small requests through a throwaway server load the batched
+    # kernels and grow the memory pools (the plain path's kernels were loaded
+    # by the error measurement above)
+    wp, wm = workloads.plummer(4096, seed=5)
+    warm = [serve.Request(-1 - k, 0.0, wp, np.zeros_like(wp), wm, steps=12) for k in range(2)]
+    sv = serve.Server(theta=theta, softening=0.01, dt=1e-3, rebuild_every=10, form="fp32",
+                      criterion=criterion, multipole=multipole)
+    sv.run(warm, realtime=False)
+    sv.close()
     sv = serve.Server(theta=theta, softening=0.01, dt=1e-3, rebuild_every=10, form="fp32",
                       criterion=criterion, multipole=multipole)
     st = sv.run(reqs, realtime=True)
