@@ -241,11 +241,13 @@ def measure_gemm_peak(torch, dtype) -> float:
 
 
 # FP32-pipe operations of one float-float pair (or monopole) term of the fast
-# form, counted from bhut_gb300/csrc/traverse_fast.cu (pair_ff, 3-D, target
-# inside the box): displacement 15, r^2 + eps^2 43, range check 2, refined
-# rsqrt and cube 11, m * w 4, three float-float products and accumulations
-# 36 -> 107 (plus one MUFU rsqrt).
-FF_OPS_PER_INTERACTION = 107
+# form, counted from bhut_gb300/csrc/fast.cuh (pair_ff, 3-D, target inside
+# the box): displacement 15 (5 per axis), r^2 + eps^2 and its low part 37
+# (error-free squares and sums), refined rsqrt and cube 11, m * w 4, three
+# float-float products and accumulations 36 -> 103 (plus one MUFU rsqrt;
+# the small-R range test and its selects are compiled out when the
+# softening bounds R from below, as in this workload).
+FF_OPS_PER_INTERACTION = 103
 # ... and of the fp32 form (fast.cuh): a pair term (pair_f32_partial:
 # displacement 9, r^2 + eps^2 3, cube 2, m * w 1, three FMAs into the leaf
 # partial 3 -> 18) and a monopole (pair_f32: the same 15 plus a Kahan step
