@@ -21,15 +21,15 @@
 //    the same time) race on the array and must not be issued;
 //  * the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress, once per device, with that device current); make
-//    that first call before any stream capture.
+//    that first call before any stream capture.  The address is kept for the
+//    life of the process, so a process that calls cudaDeviceReset must not
+//    call this entry point again afterwards;
+//  * each call ends by reading the error word back and synchronizing its
+//    stream, so a bad input is reported by the call that received it.
 #include <mutex>
 
 #include "../../include/bhut_gb300.h"
 #include "tree.cuh"
-
-namespace bhut {
-bool is_device_pointer(const void* p);
-}
 
 using namespace bhut;
 
@@ -79,6 +79,21 @@ int scratch_address(void** out)
     return kOk;
 }
 
+// True when p is device memory of device `dev` or managed memory.  Kernels
+// here dereference the caller's pointers directly, so memory of another GPU
+// (reachable only with peer access) is refused rather than faulted on.
+bool on_device(const void* p, int dev)
+{
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
+}
+
 }  // namespace
 
 extern "C" int bhut_morton_argsort_noalloc(const double* positions, int64_t n, int dim,
@@ -91,10 +106,11 @@ extern "C" int bhut_morton_argsort_noalloc(const double* positions, int64_t n, i
                   "use bhut_morton_argsort", (long long)n, (long long)kNoAllocMaxPoints);
         return kInvalid;
     }
-    if (!is_device_pointer(positions) || !is_device_pointer(sorted_keys) ||
-        !is_device_pointer(perm)) {
-        set_error("bhut_morton_argsort_noalloc needs device pointers for positions, "
-                  "sorted_keys and perm");
+    int dev = 0;
+    BHUT_CUDA(cudaGetDevice(&dev));
+    if (!on_device(positions, dev) || !on_device(sorted_keys, dev) || !on_device(perm, dev)) {
+        set_error("bhut_morton_argsort_noalloc needs device pointers of the current device "
+                  "(%d) or managed memory for positions, sorted_keys and perm", dev);
         return kInvalid;
     }
     if (sort_scratch_bytes(n) > kSortBytes) {

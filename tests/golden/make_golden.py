@@ -2,7 +2,7 @@
 
 Usage (needs the bhut 0.1.0 source tree; it is imported read-only):
 
-    BHUT_REFERENCE=/root/reference python tests/golden/make_golden.py
+    BHUT_REFERENCE=<path of the bhut source tree> python tests/golden/make_golden.py
 
 Every fixture stores the inputs (or the seed plus a digest of the inputs for
 the 1,000,000-particle case), the reference's Morton keys, permutation and
@@ -24,7 +24,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-sys.path.insert(0, os.environ.get("BHUT_REFERENCE", "/root/reference"))
+if not os.environ.get("BHUT_REFERENCE"):
+    sys.exit("set BHUT_REFERENCE to the bhut 0.1.0 source tree (the folder holding bhut/)")
+sys.path.insert(0, os.environ["BHUT_REFERENCE"])
 sys.path.insert(0, REPO)
 
 import bhut  # noqa: E402
