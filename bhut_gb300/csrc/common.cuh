@@ -53,21 +53,23 @@ inline unsigned grid_for(int64_t n, int block, unsigned cap = 152u * 16u)
 }
 
 // ---------------------------------------------------------------------------
-// Radix sort of (uint64 key, int32 value) pairs, stable, LSD, 8-bit digits.
+// Radix sort of (uint64 key, int32 value) pairs, stable, LSD, 8-bit digits
+// (sort.cu).
 // ---------------------------------------------------------------------------
-struct SortScratch {
-    uint64_t* keys_alt = nullptr;
-    int32_t* vals_alt = nullptr;
-    uint32_t* tile_counts = nullptr;   // 256 * tiles
-    uint32_t* block_sums = nullptr;    // scan partials
-    int64_t capacity = 0;
-    int64_t tile_capacity = 0;
-};
 constexpr int kSortTile = 4096;        // keys per tile (8 warps x 512)
 constexpr int kSortThreads = 256;
+constexpr int kSortPassesMax = 8;      // 64 key bits
 
-int64_t sort_tiles(int64_t n);
-size_t sort_scratch_bytes(int64_t n);
+constexpr int64_t sort_tiles(int64_t n) { return (n + kSortTile - 1) / kSortTile; }
+constexpr size_t sort_align(size_t x) { return (x + 255) & ~(size_t)255; }
+// Scratch of radix_sort_pairs for n keys: the ping-pong keys and values, two
+// bucket-major count tables (256 x tiles) and the per-pass digit totals.
+constexpr size_t sort_scratch_bytes(int64_t n)
+{
+    return sort_align(sizeof(uint64_t) * (size_t)n) + sort_align(sizeof(int32_t) * (size_t)n) +
+           2 * sort_align(sizeof(uint32_t) * 256 * (size_t)sort_tiles(n)) +
+           sort_align(sizeof(uint32_t) * 256 * kSortPassesMax);
+}
 // Sorts keys[0..n) ascending with values carried along.  `bits` is the
 // number of low key bits that can be non-zero (passes = ceil(bits / 8)).
 // The result ends in keys/vals.  Scratch must hold sort_scratch_bytes(n).

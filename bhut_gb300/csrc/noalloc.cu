@@ -37,13 +37,9 @@ namespace {
 
 constexpr int64_t kNoAllocMaxPoints = 1 << 20;          // 1,048,576 points
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-constexpr int64_t kMaxTiles = (kNoAllocMaxPoints + kSortTile - 1) / kSortTile;
-constexpr int64_t kMaxCounts = 256 * kMaxTiles;
-// Region sizes (same layout as sort_scratch_bytes for kNoAllocMaxPoints).
-constexpr size_t kSortBytes = align256(sizeof(uint64_t) * kNoAllocMaxPoints) +
-                              align256(sizeof(int32_t) * kNoAllocMaxPoints) +
-                              align256(sizeof(uint32_t) * kMaxCounts) +
-                              align256(sizeof(uint32_t) * (kMaxCounts / 4096 + 2));
+// Region sizes: the sort's scratch for kNoAllocMaxPoints keys, then the
+// bounding-box partials, the box and the counters.
+constexpr size_t kSortBytes = sort_scratch_bytes(kNoAllocMaxPoints);
 constexpr size_t kBoxPartialBytes = align256(sizeof(double) * kBoxPartialDoubles);
 constexpr size_t kBoxBytes = 256;
 constexpr size_t kWordBytes = 256;                      // counters[8] + error word
