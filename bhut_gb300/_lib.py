@@ -91,6 +91,7 @@ SIGNATURES = {
     "bhut_batch_keep_order": (_INT, [_VP, _VP, _VP]),
     "bhut_batch_order": (_INT, [_VP, _VP]),
     "bhut_batch_destroy": (None, [_VP]),
+    "bhut_batch_traverse_ms": (_INT, [_VP, _VP]),
     "bhut_leapfrog": (_INT, [_VP, _VP, _VP, _I64, _INT, _D, _D, _VP]),
 }
 

@@ -111,6 +111,13 @@ class BatchedSolver:
                                            ctypes.byref(c)))
         return a.value, b.value, c.value
 
+    def traverse_ms(self) -> float:
+        """Device time of the last solve's traversal kernel (CUDA events
+        around its launch), milliseconds."""
+        ms = ctypes.c_double()
+        _lib.check(self.L.bhut_batch_traverse_ms(self.h, ctypes.byref(ms)))
+        return ms.value
+
     def info(self):
         v = [ctypes.c_int64() for _ in range(4)]
         _lib.check(self.L.bhut_batch_info(self.h, *[ctypes.byref(x) for x in v]))

@@ -100,17 +100,29 @@ k_seg_morton(const double* __restrict__ pos, const int64_t* __restrict__ off, in
     const int s = blockIdx.x;
     const int64_t p0 = off[s], p1 = off[s + 1];
     const double* bx = box + s * 8;
-    double pmin[3], ext[3], offs[3];
-    for (int d = 0; d < 3; d++) { pmin[d] = 0.0; ext[d] = 1.0; offs[d] = 0.0; }
+    double pmin[3], ext[3], offs[3], rcp[3];
+    bool degenerate = false;
+    for (int d = 0; d < 3; d++) { pmin[d] = 0.0; ext[d] = 1.0; offs[d] = 0.0; rcp[d] = 1.0; }
     for (int d = 0; d < dim; d++) {
         pmin[d] = bx[d];
         const double e = __dsub_rn(bx[3 + d], bx[d]);
         ext[d] = e <= 0 ? 1.0 : e;
         offs[d] = e <= 0 ? 0.5 : 0.0;
+        degenerate |= e <= 0;
+        rcp[d] = __drcp_rn(ext[d]);
     }
     for (int64_t i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
         uint64_t key;
-        if (dim == 3) {
+        if (!degenerate) {   // division-free quantiser (uniform branch per system)
+            if (dim == 3) {
+                key = morton3(quantise_rcp(pos[3 * i], pmin[0], ext[0], rcp[0]),
+                              quantise_rcp(pos[3 * i + 1], pmin[1], ext[1], rcp[1]),
+                              quantise_rcp(pos[3 * i + 2], pmin[2], ext[2], rcp[2]));
+            } else {
+                key = morton2(quantise_rcp(pos[2 * i], pmin[0], ext[0], rcp[0]),
+                              quantise_rcp(pos[2 * i + 1], pmin[1], ext[1], rcp[1]));
+            }
+        } else if (dim == 3) {
             key = morton3(quantise(pos[3 * i], pmin[0], ext[0], offs[0]),
                           quantise(pos[3 * i + 1], pmin[1], ext[1], offs[1]),
                           quantise(pos[3 * i + 2], pmin[2], ext[2], offs[2]));
@@ -768,11 +780,12 @@ struct bhut_batch {
     BufB pos, mass, d_part_off, d_node_off, d_leaf_off, d_tasks, keys, perm, sys_of, key2,
         sx, sy, sz, sm, cm, size, center, half, lo, hi, first_child, start, count, parent,
         leaf_list, arrive, sort_scratch, box, frames, ph, pl, nh, nl, nsize, ndelta, counter,
-        err, stats, out, keep, perm_in, quad, nq0, nq1, nhdr, roots, forced;
+        err, stats, out, keep, perm_in, quad, nq0, nq1, nhdr, roots, forced, frontier;
     bool keep_active = false;
     unsigned long long last_stats[5] = {0, 0, 0, 0, 0};
     cudaGraphExec_t graph = nullptr;
     bool use_graph = false;
+    cudaEvent_t ev_trav[2] = {nullptr, nullptr};   // around the traversal (graph nodes too)
     double g_theta = -1, g_eps = -1, g_G = 0;
     double* g_out = nullptr;
 
@@ -783,7 +796,7 @@ struct bhut_batch {
                         &first_child, &start, &count, &parent, &leaf_list, &arrive,
                         &sort_scratch, &box, &frames, &ph, &pl, &nh, &nl, &nsize, &ndelta,
                         &counter, &err, &stats, &out, &keep, &perm_in, &quad, &nq0, &nq1, &nhdr,
-                        &roots, &forced})
+                        &roots, &forced, &frontier})
             x->release(stream);
     }
 
@@ -884,6 +897,7 @@ int plan_layout(bhut_batch* b, const int64_t* offsets, int64_t nsys)
         BHUT_TRY(x->ensure(sizeof(int32_t) * mtot, s));
     BHUT_TRY(b->arrive.ensure(sizeof(unsigned) * mtot, s));
     BHUT_TRY(b->leaf_list.ensure(sizeof(int32_t) * b->ltot, s));
+    BHUT_TRY(b->frontier.ensure(sizeof(int32_t) * b->ltot, s));
     BHUT_TRY(b->nh.ensure(sizeof(float4) * mtot, s));
     BHUT_TRY(b->nl.ensure(sizeof(float4) * mtot, s));
     BHUT_TRY(b->nsize.ensure(sizeof(float) * mtot, s));
@@ -970,6 +984,7 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
                               b->first_child.as<int32_t>(), b->start.as<int32_t>(),
                               b->count.as<int32_t>(), b->parent.as<int32_t>(),
                               b->arrive.as<unsigned>(), o, false, nullptr, nullptr,
+                              b->frontier.as<int32_t>(), b->counter.as<unsigned>() + 2,
                               b->err.as<unsigned>(), s));
     if (b->refit_rule) {
         k_seg_roots_update<<<grid_for(ns, 128), 128, 0, s>>>(
@@ -984,6 +999,7 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
                                     b->first_child.as<int32_t>(), b->start.as<int32_t>(),
                                     b->count.as<int32_t>(), b->parent.as<int32_t>(),
                                     b->arrive.as<unsigned>(), b->quad.as<double>(),
+                                    b->frontier.as<int32_t>(), b->counter.as<unsigned>() + 2,
                                     b->err.as<unsigned>(), s));
     k_seg_frames<<<(unsigned)ns, kSegThreads, 0, s>>>(
         b->dev(), b->d_part_off.as<int64_t>(), b->d_node_off.as<int64_t>(), b->box.as<double>(),
@@ -1005,6 +1021,7 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
                 eps, G, b->mac, out, b->err.as<unsigned>(), b->stats.as<unsigned long long>()};
     const bool fp32 = b->form == BHUT_FORM_FP32;
     const int stk = b->stack;
+    if (b->ev_trav[0]) BHUT_CUDA(cudaEventRecord(b->ev_trav[0], s));
     if (dim == 3) {
         if (fp32 && b->tpw == 32) launch_batch_traverse<3, true, 32>(stk, s, bd, a);
         else if (fp32) launch_batch_traverse<3, true, 16>(stk, s, bd, a);
@@ -1015,6 +1032,7 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
         else launch_batch_traverse<2, false, 32>(stk, s, bd, a);
     }
     BHUT_CUDA(cudaGetLastError());
+    if (b->ev_trav[1]) BHUT_CUDA(cudaEventRecord(b->ev_trav[1], s));
     note_launches(1);
     return kOk;
 }
@@ -1028,6 +1046,9 @@ int ensure_topology(bhut_batch* b)
         b->parent.as<int32_t>(), b->leaf_list.as<int32_t>(), b->err.as<unsigned>());
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
+    // leaves in particle order (the particle keys are free until the solve)
+    BHUT_TRY(order_leaves(b->leaf_list.as<int32_t>(), b->ltot, b->start.as<int32_t>(),
+                          b->keys.as<uint64_t>(), b->sort_scratch.p, b->stream));
     b->topo_valid = true;
     return kOk;
 }
@@ -1066,6 +1087,8 @@ int bhut_batch_create(int dim, int leaf_size, void* stream, bhut_batch** out)
         if (e != cudaSuccess) { delete b; return cuda_status(e, "cudaStreamCreate"); }
         b->own_stream = true;
     }
+    for (cudaEvent_t& e : b->ev_trav)
+        if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); e = nullptr; }
     *out = b;
     return kOk;
 }
@@ -1344,8 +1367,21 @@ void bhut_batch_destroy(bhut_batch* b)
     drop_graph(b);
     b->release_all();
     cudaStreamSynchronize(b->stream);
+    for (cudaEvent_t e : b->ev_trav)
+        if (e) cudaEventDestroy(e);
     if (b->own_stream) cudaStreamDestroy(b->stream);
     delete b;
+}
+
+int bhut_batch_traverse_ms(const bhut_batch* b, double* ms)
+{
+    if (!b || !ms) { set_error("batch or ms is NULL"); return kInvalid; }
+    if (!b->ev_trav[0] || !b->ev_trav[1]) { set_error("no traversal timing events"); return kInvalid; }
+    BHUT_CUDA(cudaEventSynchronize(b->ev_trav[1]));
+    float f = 0.0f;
+    BHUT_CUDA(cudaEventElapsedTime(&f, b->ev_trav[0], b->ev_trav[1]));
+    *ms = f;
+    return kOk;
 }
 
 }  // extern "C"

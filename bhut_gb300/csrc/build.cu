@@ -22,109 +22,164 @@
 namespace bhut {
 
 // ---------------------------------------------------------------------------
-// K1: bounding box.  Block partials, the last block to finish reduces them
-// (no waiting: a block that is not last just exits).
+// K1: bounding box.  The position array is read as a flat array of n * dim
+// doubles; the grid stride is a multiple of 6, so each thread sees one axis.
+// Minima and maxima are taken on order-preserving integer images of the
+// doubles (the FP64 pipe runs at 1/64 of the integer pipes here), which
+// give the same values as FP64 comparisons (-0.0 and +0.0 aside, which
+// compare equal).  Optionally the kernel also copies positions and masses
+// to staging buffers (one read for the copy, the finiteness check and the
+// box).  Block partials; the last block to finish reduces them (no block
+// waits on another) and adds the extents' reciprocals for the Morton
+// quantiser and per-axis NaN flags.
 // ---------------------------------------------------------------------------
-constexpr int kBoxThreads = 256;
+constexpr int kBoxThreads = 192;   // a multiple of 6 and of 32
+
+__device__ __forceinline__ uint64_t ord_key(uint64_t b)   // monotone in the double value
+{
+    return b ^ ((uint64_t)((int64_t)b >> 63) | 0x8000000000000000ull);
+}
+__device__ __forceinline__ uint64_t ord_inv(uint64_t k)
+{
+    return k ^ (((k >> 63) ? 0ull : ~0ull) | 0x8000000000000000ull);
+}
+__device__ __forceinline__ bool finite_bits(uint64_t b)
+{
+    return ((b >> 52) & 0x7ff) != 0x7ff;
+}
 
 __global__ void __launch_bounds__(kBoxThreads)
 k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t n, int dim,
+       double* __restrict__ pos_copy, double* __restrict__ mass_copy,
        double* __restrict__ partial, unsigned* __restrict__ done_counter, double* __restrict__ box,
        unsigned* __restrict__ err)
 {
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    double mmax = 0.0;
-    bool bad = false;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        for (int d = 0; d < dim; d++) {
-            double v = pos[i * dim + d];
-            bad |= !isfinite(v);
-            lo[d] = v < lo[d] ? v : lo[d];
-            hi[d] = v > hi[d] ? v : hi[d];
+    const int tid = threadIdx.x;
+    const int64_t first = blockIdx.x * (int64_t)kBoxThreads + tid;
+    const int64_t stride = (int64_t)gridDim.x * kBoxThreads;   // multiple of 6
+    const int64_t total = n * dim;
+    const int axis = (int)(first % dim);
+    const uint64_t* __restrict__ p = reinterpret_cast<const uint64_t*>(pos);
+    uint64_t* __restrict__ pc = reinterpret_cast<uint64_t*>(pos_copy);
+    uint64_t lo = ~0ull, hi = 0ull;
+    bool bad = false, nan = false;
+    // batches of kBoxBatch loads are issued before any store of the copy
+    // (the copy does not alias the input, but the compiler cannot know)
+    constexpr int kBoxBatch = 8;
+    for (int64_t j0 = first; j0 < total; j0 += kBoxBatch * stride) {
+        uint64_t b[kBoxBatch];
+#pragma unroll
+        for (int u = 0; u < kBoxBatch; u++) {
+            const int64_t j = j0 + u * stride;
+            b[u] = j < total ? __ldg(p + j) : 0ull;
         }
-        if (mass) {
-            double am = fabs(mass[i]);
-            bad |= !isfinite(am);
-            mmax = am > mmax ? am : mmax;
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        double a = __shfl_down_sync(0xffffffffu, mmax, o);
-        mmax = a > mmax ? a : mmax;
-    }
-    __shared__ double s_m[kBoxThreads / 32];
-    if ((threadIdx.x & 31) == 0) s_m[threadIdx.x >> 5] = mmax;
-    __shared__ double s_lo[3][kBoxThreads / 32], s_hi[3][kBoxThreads / 32];
-    __shared__ bool s_last;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int d = 0; d < 3; d++) {
-        for (int o = 16; o > 0; o >>= 1) {
-            double a = __shfl_down_sync(0xffffffffu, lo[d], o);
-            double b = __shfl_down_sync(0xffffffffu, hi[d], o);
-            lo[d] = a < lo[d] ? a : lo[d];
-            hi[d] = b > hi[d] ? b : hi[d];
-        }
-        if (lane == 0) { s_lo[d][warp] = lo[d]; s_hi[d][warp] = hi[d]; }
-    }
-    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(err, kErrNonFinite);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int d = 0; d < 3; d++) {
-            double a = s_lo[d][0], b = s_hi[d][0];
-            for (int w = 1; w < kBoxThreads / 32; w++) {
-                a = s_lo[d][w] < a ? s_lo[d][w] : a;
-                b = s_hi[d][w] > b ? s_hi[d][w] : b;
+#pragma unroll
+        for (int u = 0; u < kBoxBatch; u++) {
+            const int64_t j = j0 + u * stride;
+            if (j < total) {
+                if (pc) pc[j] = b[u];
+                bad |= !finite_bits(b[u]);
+                nan |= (b[u] & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+                const uint64_t k = ord_key(b[u]);
+                lo = k < lo ? k : lo;
+                hi = k > hi ? k : hi;
             }
-            partial[blockIdx.x * 8 + d] = a;
-            partial[blockIdx.x * 8 + 3 + d] = b;
         }
-        double mm = s_m[0];
-        for (int w = 1; w < kBoxThreads / 32; w++) mm = s_m[w] > mm ? s_m[w] : mm;
-        partial[blockIdx.x * 8 + 6] = mm;
+    }
+    uint64_t mm = 0ull;   // |mass| bits: non-negative doubles order as integers
+    if (mass) {
+        const uint64_t* __restrict__ q = reinterpret_cast<const uint64_t*>(mass);
+        uint64_t* __restrict__ qc = reinterpret_cast<uint64_t*>(mass_copy);
+        for (int64_t i0 = first; i0 < n; i0 += kBoxBatch * stride) {
+            uint64_t b[kBoxBatch];
+#pragma unroll
+            for (int u = 0; u < kBoxBatch; u++) {
+                const int64_t i = i0 + u * stride;
+                b[u] = i < n ? __ldg(q + i) : 0ull;
+            }
+#pragma unroll
+            for (int u = 0; u < kBoxBatch; u++) {
+                const int64_t i = i0 + u * stride;
+                if (i < n) {
+                    if (qc) qc[i] = b[u];
+                    bad |= !finite_bits(b[u]);
+                    const uint64_t a = b[u] & 0x7FFFFFFFFFFFFFFFull;
+                    mm = a > mm ? a : mm;
+                }
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, bad) && (tid & 31) == 0) atomicOr(err, kErrNonFinite);
+    __shared__ uint64_t s_lo[kBoxThreads], s_hi[kBoxThreads], s_m[kBoxThreads];
+    __shared__ bool s_last;
+    __shared__ unsigned s_nan;   // bit d: axis d holds a NaN
+    if (tid == 0) s_nan = 0;
+    s_lo[tid] = lo;
+    s_hi[tid] = hi;
+    s_m[tid] = mm;
+    __syncthreads();
+    if (nan) atomicOr(&s_nan, 1u << axis);
+    // thread d < dim reduces its axis (the threads with tid = d (mod dim):
+    // the block's first index is a multiple of 6); thread 3 the masses
+    if (tid < dim) {
+        uint64_t l = ~0ull, h = 0ull;
+        for (int t = tid; t < kBoxThreads; t += dim) {
+            l = s_lo[t] < l ? s_lo[t] : l;
+            h = s_hi[t] > h ? s_hi[t] : h;
+        }
+        partial[blockIdx.x * 8 + tid] = __longlong_as_double((long long)l);
+        partial[blockIdx.x * 8 + 3 + tid] = __longlong_as_double((long long)h);
+    } else if (tid == 3) {
+        uint64_t m = 0ull;
+        for (int t = 0; t < kBoxThreads; t++) m = s_m[t] > m ? s_m[t] : m;
+        partial[blockIdx.x * 8 + 6] = __longlong_as_double((long long)m);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        partial[blockIdx.x * 8 + 7] = (double)s_nan;
         __threadfence();
-        unsigned ticket = atomicAdd(done_counter, 1u);
+        const unsigned ticket = atomicAdd(done_counter, 1u);
         s_last = (ticket == gridDim.x - 1);
     }
     __syncthreads();
     if (!s_last) return;
-    // last block: reduce all partials in parallel (strided over blocks)
+    // last block: reduce the partials (ordered images; |mass| bits)
     __threadfence();
-    double a[7];
-    for (int d = 0; d < 3; d++) { a[d] = INFINITY; a[3 + d] = -INFINITY; }
-    a[6] = 0.0;
-    for (unsigned g = threadIdx.x; g < gridDim.x; g += blockDim.x) {
-        for (int d = 0; d < 3; d++) {
-            double x = __ldcg(&partial[g * 8 + d]), y = __ldcg(&partial[g * 8 + 3 + d]);
-            a[d] = x < a[d] ? x : a[d];
-            a[3 + d] = y > a[3 + d] ? y : a[3 + d];
-        }
-        double mm = __ldcg(&partial[g * 8 + 6]);
-        a[6] = mm > a[6] ? mm : a[6];
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        for (int d = 0; d < 3; d++) {
-            double x = __shfl_down_sync(0xffffffffu, a[d], o);
-            double y = __shfl_down_sync(0xffffffffu, a[3 + d], o);
-            a[d] = x < a[d] ? x : a[d];
-            a[3 + d] = y > a[3 + d] ? y : a[3 + d];
-        }
-        double mm = __shfl_down_sync(0xffffffffu, a[6], o);
-        a[6] = mm > a[6] ? mm : a[6];
-    }
-    __shared__ double s_fin[kBoxThreads / 32][7];
-    if (lane == 0)
-        for (int k = 0; k < 7; k++) s_fin[warp][k] = a[k];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < kBoxThreads / 32; w++) {
-            for (int d = 0; d < 3; d++) {
-                a[d] = s_fin[w][d] < a[d] ? s_fin[w][d] : a[d];
-                a[3 + d] = s_fin[w][3 + d] > a[3 + d] ? s_fin[w][3 + d] : a[3 + d];
+    if (tid < 7) {
+        const bool is_lo = tid < 3, is_m = tid == 6;
+        const int d = tid < 3 ? tid : tid - 3;
+        if (is_m || d < dim) {
+            uint64_t acc = is_lo ? ~0ull : 0ull;
+            for (unsigned g = 0; g < gridDim.x; g++) {
+                const uint64_t k = (uint64_t)__double_as_longlong(__ldcg(&partial[g * 8 + tid]));
+                if (is_lo) acc = k < acc ? k : acc;
+                else acc = k > acc ? k : acc;
             }
-            a[6] = s_fin[w][6] > a[6] ? s_fin[w][6] : a[6];
+            box[tid] = is_m ? __longlong_as_double((long long)acc)
+                            : __longlong_as_double((long long)ord_inv(acc));
+        } else {
+            box[tid] = tid < 3 ? INFINITY : -INFINITY;
         }
-        for (int k = 0; k < 7; k++) box[k] = a[k];
+    }
+    __syncthreads();
+    // per axis the reciprocal of the extent that the Morton quantiser uses
+    // (box[8 + d]), whether an axis has zero extent (box[11]) and which axes
+    // hold a NaN (box[12 + d])
+    if (tid == 0) {
+        bool degenerate = false;
+        for (int d = 0; d < 3; d++) {
+            double r = 1.0;
+            if (d < dim) {
+                const double e = __dsub_rn(box[3 + d], box[d]);
+                degenerate |= !(e > 0.0);
+                r = e > 0.0 ? __drcp_rn(e) : 1.0;
+            }
+            box[8 + d] = r;
+        }
+        box[11] = degenerate ? 1.0 : 0.0;
+        unsigned nanmask = 0;
+        for (unsigned g = 0; g < gridDim.x; g++) nanmask |= (unsigned)__ldcg(&partial[g * 8 + 7]);
+        for (int d = 0; d < 3; d++) box[12 + d] = (nanmask >> d) & 1u ? 1.0 : 0.0;
         *done_counter = 0;
     }
 }
@@ -136,23 +191,34 @@ __global__ void k_morton(const double* __restrict__ pos, int64_t n, int dim,
                          const double* __restrict__ box, uint64_t* __restrict__ keys,
                          int32_t* __restrict__ idx)
 {
-    double pmin[3], ext[3], off[3];
+    double pmin[3], ext[3], off[3], rcp[3];
     for (int d = 0; d < dim; d++) {
         pmin[d] = box[d];
         double e = __dsub_rn(box[3 + d], box[d]);
         ext[d] = e <= 0 ? 1.0 : e;
         off[d] = e <= 0 ? 0.5 : 0.0;
+        rcp[d] = box[8 + d];   // RN(1 / extent), from the bounding-box kernel
     }
+    const bool degenerate = box[11] != 0.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         uint64_t key;
-        if (dim == 3) {
-            key = morton3(quantise(pos[3 * i], pmin[0], ext[0], off[0]),
-                          quantise(pos[3 * i + 1], pmin[1], ext[1], off[1]),
-                          quantise(pos[3 * i + 2], pmin[2], ext[2], off[2]));
+        if (degenerate) {   // an axis of zero extent (uniform branch)
+            if (dim == 3) {
+                key = morton3(quantise(pos[3 * i], pmin[0], ext[0], off[0]),
+                              quantise(pos[3 * i + 1], pmin[1], ext[1], off[1]),
+                              quantise(pos[3 * i + 2], pmin[2], ext[2], off[2]));
+            } else {
+                key = morton2(quantise(pos[2 * i], pmin[0], ext[0], off[0]),
+                              quantise(pos[2 * i + 1], pmin[1], ext[1], off[1]));
+            }
+        } else if (dim == 3) {
+            key = morton3(quantise_rcp(pos[3 * i], pmin[0], ext[0], rcp[0]),
+                          quantise_rcp(pos[3 * i + 1], pmin[1], ext[1], rcp[1]),
+                          quantise_rcp(pos[3 * i + 2], pmin[2], ext[2], rcp[2]));
         } else {
-            key = morton2(quantise(pos[2 * i], pmin[0], ext[0], off[0]),
-                          quantise(pos[2 * i + 1], pmin[1], ext[1], off[1]));
+            key = morton2(quantise_rcp(pos[2 * i], pmin[0], ext[0], rcp[0]),
+                          quantise_rcp(pos[2 * i + 1], pmin[1], ext[1], rcp[1]));
         }
         keys[i] = key;
         if (idx) idx[i] = (int32_t)i;
@@ -301,17 +367,26 @@ __device__ void leaf_node(int32_t id, int dim, bool refit, const TreeDev& t,
     if (!refit) {
         auto ld = [&](int64_t i) { return t.sm[s + i]; };
         total = __dadd_rn(0.0, pairwise_sum(ld, c));
-        double lo[3], hi[3];
+        // AABB on order-preserving integer images (same values as FP64
+        // comparisons; the FP64 pipe is the scarce one); loads run ahead of
+        // the row-order sums
+        uint64_t klo[3] = {~0ull, ~0ull, ~0ull}, khi[3] = {0ull, 0ull, 0ull};
         const double* axes[3] = {t.sx, t.sy, t.sz};
-        for (int d = 0; d < dim; d++) { lo[d] = axes[d][s]; hi[d] = lo[d]; }
+#pragma unroll 4
         for (int64_t i = 0; i < c; i++) {
-            double mi = t.sm[s + i];
+            const double mi = t.sm[s + i];
             for (int d = 0; d < dim; d++) {
-                double v = axes[d][s + i];
-                lo[d] = v < lo[d] ? v : lo[d];
-                hi[d] = v > hi[d] ? v : hi[d];
+                const double v = axes[d][s + i];
+                const uint64_t k = ord_key((uint64_t)__double_as_longlong(v));
+                klo[d] = k < klo[d] ? k : klo[d];
+                khi[d] = k > khi[d] ? k : khi[d];
                 acc[d] = __dadd_rn(acc[d], __dmul_rn(mi, v));
             }
+        }
+        double lo[3], hi[3];
+        for (int d = 0; d < dim; d++) {
+            lo[d] = __longlong_as_double((long long)ord_inv(klo[d]));
+            hi[d] = __longlong_as_double((long long)ord_inv(khi[d]));
         }
         double ext = 0.0;
         for (int d = 0; d < dim; d++) {
@@ -326,6 +401,7 @@ __device__ void leaf_node(int32_t id, int dim, bool refit, const TreeDev& t,
     } else {
         auto ld = [&](int64_t i) { return omass[t.perm[s + i]]; };
         total = __dadd_rn(0.0, pairwise_sum(ld, c));
+#pragma unroll 4
         for (int64_t i = 0; i < c; i++) {
             int64_t p = t.perm[s + i];
             double mi = omass[p];
@@ -362,9 +438,12 @@ __device__ void internal_node(int32_t id, int32_t fc, int dim, bool refit, NodeO
     if (!refit) {
         double ext = 0.0;
         for (int d = 0; d < dim; d++) {
-            double l0 = __ldcg(&o.lo[3 * fc + d]), l1 = __ldcg(&o.lo[3 * (fc + 1) + d]);
-            double h0 = __ldcg(&o.hi[3 * fc + d]), h1 = __ldcg(&o.hi[3 * (fc + 1) + d]);
-            double lo = l1 < l0 ? l1 : l0, hi = h1 > h0 ? h1 : h0;
+            const uint64_t l0 = ord_key((uint64_t)__double_as_longlong(__ldcg(&o.lo[3 * fc + d])));
+            const uint64_t l1 = ord_key((uint64_t)__double_as_longlong(__ldcg(&o.lo[3 * (fc + 1) + d])));
+            const uint64_t h0 = ord_key((uint64_t)__double_as_longlong(__ldcg(&o.hi[3 * fc + d])));
+            const uint64_t h1 = ord_key((uint64_t)__double_as_longlong(__ldcg(&o.hi[3 * (fc + 1) + d])));
+            const double lo = __longlong_as_double((long long)ord_inv(l1 < l0 ? l1 : l0));
+            const double hi = __longlong_as_double((long long)ord_inv(h1 > h0 ? h1 : h0));
             o.lo[3 * id + d] = lo;
             o.hi[3 * id + d] = hi;
             o.center[dim * id + d] = __dmul_rn(__dadd_rn(lo, hi), 0.5);
@@ -401,42 +480,159 @@ __device__ void internal_node(int32_t id, int32_t fc, int dim, bool refit, NodeO
     o.cm[id] = NodeCM{com[0], com[1], com[2], total};
 }
 
-__global__ void k_bottom_up(TreeDev t, const int32_t* __restrict__ leaf_list, int64_t num_leaves,
-                            const int32_t* __restrict__ first_child,
-                            const int32_t* __restrict__ start, const int32_t* __restrict__ count,
-                            const int32_t* __restrict__ parent, unsigned* __restrict__ arrive,
-                            NodeOut o, bool refit, const double* __restrict__ opos,
-                            const double* __restrict__ omass, unsigned* __restrict__ err)
+// Leaves are taken in groups of kBuThreads consecutive entries of the leaf
+// list (one thread each).  Inside the group the lowest kBuLevels levels are
+// merged in shared memory: threads i and i ^ 2^j holding the two children of
+// one node pair up and the lower one computes the parent (the block barrier
+// orders the children's writes; no atomics, no device-wide fences).  A
+// thread left without a partner -- its sibling is in another group, or the
+// tree is irregular there -- hands its node to the frontier list, from
+// which k_bottom_up_top finishes the tree.
+constexpr int kBuThreads = 256;
+constexpr int kBuLevels = 8;   // log2(kBuThreads)
+static_assert((1 << kBuLevels) == kBuThreads, "group size is 2^kBuLevels");
+
+__device__ __forceinline__ bool bad_parent(const TreeDev& t, const int32_t* first_child, int32_t p)
 {
-    for (int64_t li = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; li < num_leaves;
-         li += (int64_t)gridDim.x * blockDim.x) {
-        int32_t id = leaf_list[li];
-        if (id < 0 || id >= t.m || start[id] < 0 || count[id] < 1 ||
-            (int64_t)start[id] + count[id] > t.n) {
+    return p >= t.m || (p >= 0 && (first_child[p] < 1 || first_child[p] + 1 >= t.m));
+}
+
+// Node operations of a bottom-up pass: the moments (build and refit modes)
+// or the quadrupoles.
+struct MomentOps {
+    TreeDev t;
+    NodeOut o;
+    bool refit;
+    const double* opos;
+    const double* omass;
+    const int32_t* start;
+    const int32_t* count;
+    __device__ void leaf(int32_t id) const { leaf_node(id, t.dim, refit, t, opos, omass, start, count, o); }
+    __device__ void internal(int32_t p, int32_t fc) const { internal_node(p, fc, t.dim, refit, o); }
+};
+
+template <class Ops>
+__global__ void __launch_bounds__(kBuThreads)
+k_bottom_up(Ops ops, TreeDev t, const int32_t* __restrict__ leaf_list, int64_t num_leaves,
+            const int32_t* __restrict__ first_child, const int32_t* __restrict__ start,
+            const int32_t* __restrict__ count, const int32_t* __restrict__ parent,
+            int32_t* __restrict__ frontier, unsigned* __restrict__ frontier_count,
+            unsigned* __restrict__ err)
+{
+    __shared__ int32_t s_par[kBuThreads];
+    __shared__ int s_alive[kBuThreads];
+    const int tid = threadIdx.x;
+    for (int64_t base = (int64_t)blockIdx.x * kBuThreads; base < num_leaves;
+         base += (int64_t)gridDim.x * kBuThreads) {
+        const int64_t li = base + tid;
+        const int32_t id = li < num_leaves ? leaf_list[li] : -1;
+        bool alive = li < num_leaves;
+        if (alive && (id < 0 || id >= t.m || start[id] < 0 || count[id] < 1 ||
+                      (int64_t)start[id] + count[id] > t.n)) {
             atomicOr(err, kErrBadNode);
-            continue;
+            alive = false;
         }
-        leaf_node(id, t.dim, refit, t, opos, omass, start, count, o);
-        // climb: each step is taken by the second child to arrive; a tree
-        // deeper than kMaxClimb (or parent links with a cycle, possible in
-        // an imported TreeData) stops with an error instead of looping
+        if (alive) ops.leaf(id);
         int32_t node = id;
-        for (int step = 0;; step++) {
-            if (step >= kMaxClimb) { atomicOr(err, kErrBadNode); break; }
-            int32_t p = parent[node];
-            if (p < 0) break;
-            if (p >= t.m || first_child[p] < 1 || first_child[p] + 1 >= t.m) {
-                atomicOr(err, kErrBadNode);
-                break;
+        bool hand_over = false;
+        for (int j = 0; j < kBuLevels; j++) {
+            int32_t p = -1;
+            if (alive) {
+                p = parent[node];
+                if (bad_parent(t, first_child, p)) {
+                    atomicOr(err, kErrBadNode);
+                    alive = false;
+                    p = -1;
+                }
             }
-            __threadfence();
-            unsigned prev = atomicAdd(&arrive[p], 1u);
+            s_par[tid] = p;
+            s_alive[tid] = alive;
+            __syncthreads();
+            const int partner = tid ^ (1 << j);
+            const bool pair = alive && s_alive[partner] && p >= 0 && s_par[partner] == p;
+            if (alive && !pair) {   // the parent is completed elsewhere (or this is the root)
+                hand_over = p >= 0;
+                alive = false;
+            }
+            if (pair) {
+                if ((tid >> j) & 1) {
+                    alive = false;
+                } else {
+                    ops.internal(p, first_child[p]);
+                    node = p;
+                }
+            }
+            __syncthreads();
+        }
+        if (alive) hand_over = parent[node] >= 0;
+        if (hand_over) {
+            const unsigned k = atomicAdd(frontier_count, 1u);
+            if (k < (unsigned)num_leaves) frontier[k] = node;
+            else atomicOr(err, kErrBadNode);
+        }
+    }
+}
+
+// The rest of the tree, from the frontier nodes up, by one block: each
+// climb step is taken by the second child to arrive at a parent (arrival
+// counters).  All climbers run in this block, so block-scope fences order
+// a child's writes before its arrival.  A climb longer than kMaxClimb
+// (parent links with a cycle, possible in an imported TreeData) stops with
+// an error instead of looping.
+constexpr int kBuTopThreads = 1024;
+
+template <class Ops>
+__global__ void __launch_bounds__(kBuTopThreads)
+k_bottom_up_top(Ops ops, TreeDev t, const int32_t* __restrict__ first_child,
+                const int32_t* __restrict__ parent, unsigned* __restrict__ arrive,
+                const int32_t* __restrict__ frontier,
+                const unsigned* __restrict__ frontier_count, int64_t cap,
+                unsigned* __restrict__ err)
+{
+    const unsigned nf = min(*frontier_count, (unsigned)cap);
+    for (unsigned f = threadIdx.x; f < nf; f += blockDim.x) {
+        int32_t node = frontier[f];
+        for (int step = 0;; step++) {
+            if (step >= kMaxClimb || node < 0 || node >= t.m) { atomicOr(err, kErrBadNode); break; }
+            const int32_t p = parent[node];
+            if (p < 0) break;
+            if (bad_parent(t, first_child, p)) { atomicOr(err, kErrBadNode); break; }
+            __threadfence_block();
+            const unsigned prev = atomicAdd_block(&arrive[p], 1u);
             if (prev == 0) break;
-            __threadfence();
-            internal_node(p, first_child[p], t.dim, refit, o);
+            __threadfence_block();
+            ops.internal(p, first_child[p]);
             node = p;
         }
     }
+}
+
+template <class Ops>
+int launch_climb(const Ops& ops, const TreeDev& t, const int32_t* leaf_list, int64_t num_leaves,
+                 const int32_t* first_child, const int32_t* start, const int32_t* count,
+                 const int32_t* parent, unsigned* arrive, int32_t* frontier,
+                 unsigned* frontier_count, unsigned* err, cudaStream_t s)
+{
+    BHUT_CUDA(cudaMemsetAsync(arrive, 0, sizeof(unsigned) * (size_t)t.m, s));
+    BHUT_CUDA(cudaMemsetAsync(frontier_count, 0, sizeof(unsigned), s));
+    const unsigned groups = (unsigned)((num_leaves + kBuThreads - 1) / kBuThreads);
+    k_bottom_up<Ops><<<groups < 152u * 8u ? groups : 152u * 8u, kBuThreads, 0, s>>>(
+        ops, t, leaf_list, num_leaves, first_child, start, count, parent, frontier,
+        frontier_count, err);
+    k_bottom_up_top<Ops><<<1, kBuTopThreads, 0, s>>>(ops, t, first_child, parent, arrive,
+                                                     frontier, frontier_count, num_leaves, err);
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(2);
+    return kOk;
+}
+
+// Sort keys for ordering the leaf list by first particle (once per topology).
+__global__ void k_leaf_keys(const int32_t* __restrict__ leaf_list, int64_t num_leaves,
+                            const int32_t* __restrict__ start, uint64_t* __restrict__ keys)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < num_leaves;
+         i += (int64_t)gridDim.x * blockDim.x)
+        keys[i] = (uint64_t)(uint32_t)start[leaf_list[i]];
 }
 
 // Traceless quadrupole of every node about its centre of mass,
@@ -456,61 +652,42 @@ __device__ __forceinline__ void quad_add(double* q, double m, double dx, double 
     q[5] += m * (3.0 * dy * dz);
 }
 
-__global__ void k_quadrupoles(TreeDev t, const int32_t* __restrict__ leaf_list, int64_t num_leaves,
-                              const int32_t* __restrict__ first_child,
-                              const int32_t* __restrict__ start, const int32_t* __restrict__ count,
-                              const int32_t* __restrict__ parent, unsigned* __restrict__ arrive,
-                              double* __restrict__ quad, unsigned* __restrict__ err)
-{
-    for (int64_t li = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; li < num_leaves;
-         li += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t id = leaf_list[li];
-        if (id < 0 || id >= t.m) { atomicOr(err, kErrBadNode); continue; }
+struct QuadOps {
+    TreeDev t;
+    double* quad;
+    const int32_t* start;
+    const int32_t* count;
+    __device__ void leaf(int32_t id) const
+    {
         const NodeCM c = t.cm[id];
         double q[6] = {0, 0, 0, 0, 0, 0};
         const int64_t s = start[id], n = count[id];
         for (int64_t i = s; i < s + n; i++)
             quad_add(q, t.sm[i], t.sx[i] - c.x, t.sy[i] - c.y, t.dim == 3 ? t.sz[i] - c.z : 0.0);
         for (int k = 0; k < 6; k++) quad[6 * (int64_t)id + k] = q[k];
-        int32_t node = id;
-        for (int step = 0;; step++) {
-            if (step >= kMaxClimb) { atomicOr(err, kErrBadNode); break; }
-            const int32_t p = parent[node];
-            if (p < 0) break;
-            if (p >= t.m || first_child[p] < 1 || first_child[p] + 1 >= t.m) {
-                atomicOr(err, kErrBadNode);
-                break;
-            }
-            __threadfence();
-            if (atomicAdd(&arrive[p], 1u) == 0) break;
-            __threadfence();
-            const NodeCM cp = t.cm[p];
-            double qp[6] = {0, 0, 0, 0, 0, 0};
-            for (int j = 0; j < 2; j++) {
-                const int32_t ch = first_child[p] + j;
-                const double2 a = __ldcg(reinterpret_cast<const double2*>(&t.cm[ch]));
-                const double2 b = __ldcg(reinterpret_cast<const double2*>(&t.cm[ch]) + 1);
-                for (int k = 0; k < 6; k++) qp[k] += __ldcg(&quad[6 * (int64_t)ch + k]);
-                quad_add(qp, b.y, a.x - cp.x, a.y - cp.y, t.dim == 3 ? b.x - cp.z : 0.0);
-            }
-            for (int k = 0; k < 6; k++) quad[6 * (int64_t)p + k] = qp[k];
-            node = p;
-        }
     }
-}
+    __device__ void internal(int32_t p, int32_t fc) const
+    {
+        const NodeCM cp = t.cm[p];
+        double qp[6] = {0, 0, 0, 0, 0, 0};
+        for (int j = 0; j < 2; j++) {
+            const int32_t ch = fc + j;
+            const double2 a = __ldcg(reinterpret_cast<const double2*>(&t.cm[ch]));
+            const double2 b = __ldcg(reinterpret_cast<const double2*>(&t.cm[ch]) + 1);
+            for (int k = 0; k < 6; k++) qp[k] += __ldcg(&quad[6 * (int64_t)ch + k]);
+            quad_add(qp, b.y, a.x - cp.x, a.y - cp.y, t.dim == 3 ? b.x - cp.z : 0.0);
+        }
+        for (int k = 0; k < 6; k++) quad[6 * (int64_t)p + k] = qp[k];
+    }
+};
 
 int launch_quadrupoles(const TreeDev& t, const int32_t* leaf_list, int64_t num_leaves,
                        const int32_t* first_child, const int32_t* start, const int32_t* count,
-                       const int32_t* parent, unsigned* arrive, double* quad, unsigned* err,
-                       cudaStream_t s)
+                       const int32_t* parent, unsigned* arrive, double* quad, int32_t* frontier,
+                       unsigned* frontier_count, unsigned* err, cudaStream_t s)
 {
-    BHUT_CUDA(cudaMemsetAsync(arrive, 0, sizeof(unsigned) * (size_t)t.m, s));
-    k_quadrupoles<<<grid_for(num_leaves, 128), 128, 0, s>>>(t, leaf_list, num_leaves, first_child,
-                                                            start, count, parent, arrive, quad,
-                                                            err);
-    BHUT_CUDA(cudaGetLastError());
-    note_launches(1);
-    return kOk;
+    return launch_climb(QuadOps{t, quad, start, count}, t, leaf_list, num_leaves, first_child,
+                        start, count, parent, arrive, frontier, frontier_count, err, s);
 }
 
 // Refit-vs-rebuild test of refit.py:236-249: any particle with
@@ -571,8 +748,16 @@ int make_topo_tables(int64_t n, int leaf_size, TopoTables* t)
 int launch_bbox(const double* pos, const double* mass, int64_t n, int dim, double* partial,
                 unsigned* counter, double* box, unsigned* err, cudaStream_t s)
 {
-    unsigned g = grid_for(n, kBoxThreads, kBoxMaxBlocks);
-    k_bbox<<<g, kBoxThreads, 0, s>>>(pos, mass, n, dim, partial, counter, box, err);
+    return launch_stage_bbox(pos, mass, n, dim, nullptr, nullptr, partial, counter, box, err, s);
+}
+
+int launch_stage_bbox(const double* pos, const double* mass, int64_t n, int dim, double* pos_copy,
+                      double* mass_copy, double* partial, unsigned* counter, double* box,
+                      unsigned* err, cudaStream_t s)
+{
+    unsigned g = grid_for(n * dim, kBoxThreads * 4, kBoxMaxBlocks);
+    k_bbox<<<g, kBoxThreads, 0, s>>>(pos, mass, n, dim, pos_copy, mass_copy, partial, counter,
+                                     box, err);
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
     return kOk;
@@ -608,18 +793,24 @@ int launch_topology(const TopoTables& tt, int32_t* first_child, int32_t* start, 
     return kOk;
 }
 
+int order_leaves(int32_t* leaf_list, int64_t num_leaves, const int32_t* start, uint64_t* keys,
+                 void* sort_scratch, cudaStream_t s)
+{
+    k_leaf_keys<<<grid_for(num_leaves, 256), 256, 0, s>>>(leaf_list, num_leaves, start, keys);
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
+    return radix_sort_pairs(keys, leaf_list, num_leaves, 31, sort_scratch, s);
+}
+
 int launch_bottom_up(const TreeDev& t, const int32_t* leaf_list, int64_t num_leaves,
                      const int32_t* first_child, const int32_t* start, const int32_t* count,
                      const int32_t* parent, unsigned* arrive, NodeOut o, bool refit,
-                     const double* opos, const double* omass, unsigned* err, cudaStream_t s)
+                     const double* opos, const double* omass, int32_t* frontier,
+                     unsigned* frontier_count, unsigned* err, cudaStream_t s)
 {
-    BHUT_CUDA(cudaMemsetAsync(arrive, 0, sizeof(unsigned) * (size_t)t.m, s));
-    k_bottom_up<<<grid_for(num_leaves, 128), 128, 0, s>>>(t, leaf_list, num_leaves, first_child,
-                                                          start, count, parent, arrive, o, refit,
-                                                          opos, omass, err);
-    BHUT_CUDA(cudaGetLastError());
-    note_launches(1);
-    return kOk;
+    return launch_climb(MomentOps{t, o, refit, opos, omass, start, count}, t, leaf_list,
+                        num_leaves, first_child, start, count, parent, arrive, frontier,
+                        frontier_count, err, s);
 }
 
 int launch_outside_root(const double* pos, int64_t n, int dim, const double* center0,

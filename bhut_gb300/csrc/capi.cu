@@ -1,5 +1,6 @@
 // C ABI of the engine (include/bhut_gb300.h): tree handles, host/device
 // pointer staging, and the build / refit / traversal pipelines.
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -92,6 +93,20 @@ int stage_in(DevBuf& dst, const void* src, size_t bytes, cudaStream_t s)
 
 using namespace bhut;
 
+// A build captured as a CUDA graph, with the buffers and sizes it was
+// captured for.
+struct BuildGraph {
+    static constexpr int kKey = 28;
+    cudaGraphExec_t exec = nullptr;
+    const void* key[kKey] = {};
+    long long launches = 0;
+    void reset()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+    }
+};
+
 struct bhut_tree {
     int dim = 3;
     int leaf = 32;
@@ -110,6 +125,12 @@ struct bhut_tree {
     DevBuf cm, size, center, half, lo, hi, first_child, start, count, parent, leaf_list, arrive;
     // scratch
     DevBuf sort_scratch, box_partial, box, counters, err, stats;
+    DevBuf frontier;          // bottom-up scratch: one entry per leaf
+    DevBuf box_in;            // bounding box of pos_in, computed while staging
+    bool box_in_valid = false;
+    BuildGraph graphs[2];     // captured builds (see do_build)
+    int graph_next = 0;
+    bool graph_unsupported = false;
     unsigned long long last_stats[5] = {0, 0, 0, 0, 0};
     // traversal targets
     DevBuf tpos, tkeys, tperm, tx, ty, tz, tbox, out;
@@ -183,6 +204,45 @@ int sort_points(bhut_tree* t, const double* dpos, const double* dmass, int64_t n
     return kOk;
 }
 
+// Kernels of one build after its buffers exist: Morton keys, radix sort,
+// Morton-ordered copies, node moments.  Captured into a CUDA graph by
+// do_build (enqueue only: no allocation, no host synchronisation).
+int enqueue_build(bhut_tree* t, int64_t n)
+{
+    cudaStream_t s = t->stream;
+    const int dim = t->dim;
+    BHUT_TRY(launch_morton(t->pos.as<double>(), n, dim, t->box.as<double>(),
+                           t->keys.as<uint64_t>(), t->perm.as<int32_t>(), s));
+    BHUT_TRY(radix_sort_pairs(t->keys.as<uint64_t>(), t->perm.as<int32_t>(), n,
+                              dim == 3 ? 63 : 42, t->sort_scratch.p, s));
+    BHUT_TRY(launch_gather(t->pos.as<double>(), t->mass.as<double>(), t->perm.as<int32_t>(), n, dim,
+                           t->sx.as<double>(), t->sy.as<double>(), t->sz.as<double>(),
+                           t->sm.as<double>(), s));
+    BHUT_TRY(launch_bottom_up(t->dev(), t->leaf_list.as<int32_t>(), t->tt.num_leaves,
+                              t->first_child.as<int32_t>(), t->start.as<int32_t>(),
+                              t->count.as<int32_t>(), t->parent.as<int32_t>(),
+                              t->arrive.as<unsigned>(), t->nodes(), false, nullptr, nullptr,
+                              t->frontier.as<int32_t>(), t->counters.as<unsigned>() + 6,
+                              t->err.as<unsigned>(), s));
+    return kOk;
+}
+
+// The buffers a build graph reads and writes, plus its sizes: a captured
+// graph is replayed only while all of them are unchanged.
+void build_graph_key(const bhut_tree* t, int64_t n, const void** key)
+{
+    const DevBuf* bufs[] = {&t->pos, &t->mass, &t->box, &t->keys, &t->perm, &t->sort_scratch,
+                            &t->sx, &t->sy, &t->sz, &t->sm, &t->cm, &t->size, &t->center,
+                            &t->half, &t->lo, &t->hi, &t->arrive, &t->first_child, &t->start,
+                            &t->count, &t->parent, &t->leaf_list, &t->err, &t->counters,
+                            &t->frontier};
+    int k = 0;
+    for (const DevBuf* b : bufs) key[k++] = b->p;
+    key[k++] = (const void*)(intptr_t)n;
+    key[k++] = (const void*)(intptr_t)t->tt.num_leaves;
+    key[k++] = (const void*)t->stream;
+}
+
 int do_build(bhut_tree* t, int64_t n)
 {
     cudaStream_t s = t->stream;
@@ -194,17 +254,20 @@ int do_build(bhut_tree* t, int64_t n)
     t->n = n;
     t->m = t->tt.num_nodes;
     const int64_t m = t->m;
-    BHUT_TRY(sort_points(t, t->pos.as<double>(), t->mass.as<double>(), n, t->keys, t->perm, t->box));
+    // every buffer first (no allocation may happen inside a captured graph)
+    BHUT_TRY(t->keys.ensure(sizeof(uint64_t) * n, s));
+    BHUT_TRY(t->perm.ensure(sizeof(int32_t) * n, s));
+    BHUT_TRY(t->box.ensure(sizeof(double) * kBoxDoubles, s));
+    BHUT_TRY(t->box_partial.ensure(sizeof(double) * kBoxPartialDoubles, s));
+    BHUT_TRY(t->sort_scratch.ensure(sort_scratch_bytes(n), s));
     for (DevBuf* b : {&t->sx, &t->sy, &t->sz, &t->sm}) BHUT_TRY(b->ensure(sizeof(double) * n, s));
-    BHUT_TRY(launch_gather(t->pos.as<double>(), t->mass.as<double>(), t->perm.as<int32_t>(), n, dim,
-                           t->sx.as<double>(), t->sy.as<double>(), t->sz.as<double>(),
-                           t->sm.as<double>(), s));
     BHUT_TRY(t->cm.ensure(sizeof(NodeCM) * m, s));
     for (DevBuf* b : {&t->size, &t->half}) BHUT_TRY(b->ensure(sizeof(double) * m, s));
     BHUT_TRY(t->center.ensure(sizeof(double) * m * dim, s));
     BHUT_TRY(t->lo.ensure(sizeof(double) * m * 3, s));
     BHUT_TRY(t->hi.ensure(sizeof(double) * m * 3, s));
     BHUT_TRY(t->arrive.ensure(sizeof(unsigned) * m, s));
+    BHUT_TRY(t->frontier.ensure(sizeof(int32_t) * m, s));
     if (!t->topo_valid) {
         for (DevBuf* b : {&t->first_child, &t->start, &t->count, &t->parent})
             BHUT_TRY(b->ensure(sizeof(int32_t) * m, s));
@@ -213,13 +276,73 @@ int do_build(bhut_tree* t, int64_t n)
                                  t->count.as<int32_t>(), t->parent.as<int32_t>(),
                                  t->leaf_list.as<int32_t>(), t->counters.as<unsigned>() + 1,
                                  t->err.as<unsigned>(), s));
+        BHUT_TRY(t->tkeys.ensure(sizeof(uint64_t) * t->tt.num_leaves, s));
+        BHUT_TRY(order_leaves(t->leaf_list.as<int32_t>(), t->tt.num_leaves,
+                              t->start.as<int32_t>(), t->tkeys.as<uint64_t>(),
+                              t->sort_scratch.p, s));
         t->topo_valid = true;
     }
-    BHUT_TRY(launch_bottom_up(t->dev(), t->leaf_list.as<int32_t>(), t->tt.num_leaves,
-                              t->first_child.as<int32_t>(), t->start.as<int32_t>(),
-                              t->count.as<int32_t>(), t->parent.as<int32_t>(),
-                              t->arrive.as<unsigned>(), t->nodes(), false, nullptr, nullptr,
-                              t->err.as<unsigned>(), s));
+    // the box of these positions was computed while they were staged
+    if (t->box_in_valid) {
+        std::swap(t->box, t->box_in);
+    } else {
+        BHUT_TRY(launch_bbox(t->pos.as<double>(), t->mass.as<double>(), n, dim,
+                             t->box_partial.as<double>(), t->counters.as<unsigned>(),
+                             t->box.as<double>(), t->err.as<unsigned>(), s));
+    }
+    t->box_in_valid = false;
+    // replay a captured graph of this exact buffer set; capture one when the
+    // same buffer set comes back (a handle built once, as by
+    // accelerations(), launches its kernels directly); two are kept: staging
+    // alternates between two position buffers
+    const void* key[BuildGraph::kKey];
+    build_graph_key(t, n, key);
+    BuildGraph* g = nullptr;
+    BuildGraph* seen = nullptr;
+    for (BuildGraph& c : t->graphs) {
+        if (std::equal(key, key + BuildGraph::kKey, c.key)) {
+            if (c.exec) g = &c;
+            else seen = &c;
+        }
+    }
+    if (!g && (!seen || t->graph_unsupported)) {
+        BuildGraph& slot = seen ? *seen : t->graphs[t->graph_next];
+        if (!seen) t->graph_next ^= 1;
+        slot.reset();
+        std::copy(key, key + BuildGraph::kKey, slot.key);   // remembered, not captured
+        BHUT_TRY(enqueue_build(t, n));
+    } else if (!g) {
+        BuildGraph& slot = *seen;
+        const long long l0 = bhut_launch_count();
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            int st = enqueue_build(t, n);
+            e = cudaStreamEndCapture(s, &graph);
+            if (st != kOk) {
+                if (e == cudaSuccess && graph) cudaGraphDestroy(graph);
+                return st;
+            }
+            if (e == cudaSuccess) {
+                e = cudaGraphInstantiate(&slot.exec, graph, 0);
+                cudaGraphDestroy(graph);
+            }
+        }
+        if (e == cudaSuccess) {
+            slot.launches = bhut_launch_count() - l0;
+            g = &slot;
+        } else {
+            // a stream that cannot be captured (e.g. the legacy default
+            // stream): launch the kernels directly from now on
+            cudaGetLastError();
+            slot.reset();
+            t->graph_unsupported = true;
+            BHUT_TRY(enqueue_build(t, n));
+        }
+    } else {
+        note_launches(g->launches);
+    }
+    if (g) BHUT_CUDA(cudaGraphLaunch(g->exec, s));
     t->ff_valid = false;
     int st = check_err_word(t, "build");
     if (st != kOk) {
@@ -245,13 +368,40 @@ int load_particles(bhut_tree* t, const double* positions, const double* masses, 
         set_error("masses are required when the particle count changes");
         return kInvalid;
     }
-    // stage and check first: a rejected input leaves the built tree intact
+    // stage and check first: a rejected input leaves the built tree intact.
+    // One kernel copies device inputs into the staging buffers, checks them
+    // for NaN/Inf and computes their bounding box (host inputs are copied
+    // in first and then only read).
     cudaStream_t s = t->stream;
-    BHUT_TRY(stage_in(t->pos_in, positions, sizeof(double) * n * t->dim, s));
-    if (masses) BHUT_TRY(stage_in(t->mass_in, masses, sizeof(double) * n, s));
+    const size_t pbytes = sizeof(double) * n * t->dim;
+    BHUT_TRY(t->pos_in.ensure(pbytes, s));
+    const double* psrc = t->pos_in.as<double>();
+    double* pcopy = nullptr;
+    if (is_device_pointer(positions)) {
+        psrc = positions;
+        pcopy = t->pos_in.as<double>();
+    } else {
+        BHUT_CUDA(cudaMemcpyAsync(t->pos_in.p, positions, pbytes, cudaMemcpyHostToDevice, s));
+    }
+    const double* msrc = t->mass.as<double>();   // masses=None: the current masses
+    double* mcopy = nullptr;
+    if (masses) {
+        BHUT_TRY(t->mass_in.ensure(sizeof(double) * n, s));
+        msrc = t->mass_in.as<double>();
+        if (is_device_pointer(masses)) {
+            msrc = masses;
+            mcopy = t->mass_in.as<double>();
+        } else {
+            BHUT_CUDA(cudaMemcpyAsync(t->mass_in.p, masses, sizeof(double) * n,
+                                      cudaMemcpyHostToDevice, s));
+        }
+    }
     unsigned* flag = t->counters.as<unsigned>() + 4;
-    BHUT_TRY(launch_check_finite(t->pos_in.as<double>(), n * t->dim,
-                                 masses ? t->mass_in.as<double>() : nullptr, n, flag, s));
+    BHUT_CUDA(cudaMemsetAsync(flag, 0, sizeof(unsigned), s));
+    BHUT_TRY(t->box_in.ensure(sizeof(double) * kBoxDoubles, s));
+    BHUT_TRY(t->box_partial.ensure(sizeof(double) * kBoxPartialDoubles, s));
+    BHUT_TRY(launch_stage_bbox(psrc, msrc, n, t->dim, pcopy, mcopy, t->box_partial.as<double>(),
+                               t->counters.as<unsigned>(), t->box_in.as<double>(), flag, s));
     unsigned bad = 0;
     BHUT_CUDA(cudaMemcpyAsync(&bad, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     BHUT_CUDA(cudaStreamSynchronize(s));
@@ -261,6 +411,7 @@ int load_particles(bhut_tree* t, const double* positions, const double* masses, 
     }
     std::swap(t->pos, t->pos_in);
     if (masses) std::swap(t->mass, t->mass_in);
+    t->box_in_valid = true;
     return kOk;
 }
 
@@ -315,6 +466,7 @@ int prepare_fast(bhut_tree* t)
                                     t->first_child.as<int32_t>(), t->start.as<int32_t>(),
                                     t->count.as<int32_t>(), t->parent.as<int32_t>(),
                                     t->arrive.as<unsigned>(), t->quad.as<double>(),
+                                    t->frontier.as<int32_t>(), t->counters.as<unsigned>() + 6,
                                     t->err.as<unsigned>(), s));
     }
     BHUT_TRY(launch_fast_prepare(t->box.as<double>(), t->dim, t->frame.as<FastFrame>(), t->dev(),
@@ -484,7 +636,8 @@ int bhut_tree_refit(bhut_tree* t, const double* positions, const double* masses,
                               t->first_child.as<int32_t>(), t->start.as<int32_t>(),
                               t->count.as<int32_t>(), t->parent.as<int32_t>(),
                               t->arrive.as<unsigned>(), t->nodes(), true, t->pos.as<double>(),
-                              t->mass.as<double>(), t->err.as<unsigned>(), s));
+                              t->mass.as<double>(), t->frontier.as<int32_t>(),
+                              t->counters.as<unsigned>() + 6, t->err.as<unsigned>(), s));
     t->ff_valid = false;
     return check_err_word(t, "refit");
 }
@@ -510,7 +663,8 @@ int bhut_tree_refit_only(bhut_tree* t, const double* positions, const double* ma
                               t->first_child.as<int32_t>(), t->start.as<int32_t>(),
                               t->count.as<int32_t>(), t->parent.as<int32_t>(),
                               t->arrive.as<unsigned>(), t->nodes(), true, t->pos.as<double>(),
-                              t->mass.as<double>(), t->err.as<unsigned>(), s));
+                              t->mass.as<double>(), t->frontier.as<int32_t>(),
+                              t->counters.as<unsigned>() + 6, t->err.as<unsigned>(), s));
     t->ff_valid = false;
     return check_err_word(t, "refit");
 }
@@ -677,9 +831,11 @@ void bhut_tree_destroy(bhut_tree* t)
                      &t->sort_scratch, &t->box_partial, &t->box, &t->counters, &t->err, &t->stats,
                      &t->tpos, &t->tkeys, &t->tperm, &t->tx, &t->ty, &t->tz, &t->tbox, &t->out,
                      &t->frame, &t->ph, &t->pl, &t->nh, &t->nl, &t->nsize, &t->ndelta, &t->th,
-                     &t->tl, &t->quad, &t->nq0, &t->nq1, &t->nhdr, &t->pos_in, &t->mass_in};
+                     &t->tl, &t->quad, &t->nq0, &t->nq1, &t->nhdr, &t->pos_in, &t->mass_in,
+                     &t->box_in, &t->frontier};
     for (DevBuf* b : all) b->release(s);
     cudaStreamSynchronize(s);
+    for (BuildGraph& g : t->graphs) g.reset();
     if (t->own_stream) cudaStreamDestroy(s);
     delete t;
 }
@@ -812,12 +968,14 @@ int bhut_aabb(const double* points, int64_t n, int dim, double* pmin, double* pm
         if (e != cudaSuccess) rc = cuda_status(e, "copy box");
     }
     // the non-finite flag of the bbox kernel is not an error here: numpy's
-    // min/max propagate NaN, and so does the copy below
+    // min/max propagate NaN (an axis holding one gets NaN bounds) and order
+    // infinities like any value
     if (rc == kOk) {
         cudaMemsetAsync(t->err.p, 0, sizeof(unsigned), s);
         for (int d = 0; d < dim; d++) {
-            pmin[d] = box[d];
-            pmax[d] = box[3 + d];
+            const bool has_nan = box[12 + d] != 0.0;
+            pmin[d] = has_nan ? NAN : box[d];
+            pmax[d] = has_nan ? NAN : box[3 + d];
         }
     }
     bhut_tree_destroy(t);
@@ -1036,7 +1194,8 @@ int bhut_tree_import(bhut_tree* t, const double* positions, const double* masses
     if (rc == kOk) rc = stage_in(ms, mass, md, s);
     if (rc == kOk) rc = stage_in(cmn, com, md * dim, s);
     if (rc == kOk) rc = stage_in(cen, center, md * dim, s);
-    for (DevBuf* b : {&t->first_child, &t->start, &t->count, &t->parent, &t->leaf_list})
+    for (DevBuf* b : {&t->first_child, &t->start, &t->count, &t->parent, &t->leaf_list,
+                      &t->frontier})
         if (rc == kOk) rc = b->ensure(sizeof(int32_t) * m, s);
     if (rc == kOk) rc = t->cm.ensure(sizeof(NodeCM) * m, s);
     for (DevBuf* b : {&t->size, &t->half})

@@ -147,26 +147,6 @@ int launch_widen_i32(const int32_t* in, int64_t n, int64_t* out, cudaStream_t s)
 }
 
 // Non-finite check of n doubles (and, optionally, m more): flag <- 1.
-__global__ void k_check_finite(const double* __restrict__ a, int64_t n,
-                               const double* __restrict__ b, int64_t m, unsigned* __restrict__ flag)
-{
-    bool bad = false;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n + m;
-         i += (int64_t)gridDim.x * blockDim.x)
-        bad |= !isfinite(i < n ? a[i] : b[i - n]);
-    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
-}
-
-int launch_check_finite(const double* a, int64_t n, const double* b, int64_t m, unsigned* flag,
-                        cudaStream_t s)
-{
-    BHUT_CUDA(cudaMemsetAsync(flag, 0, sizeof(unsigned), s));
-    k_check_finite<<<grid_for(n + m, 256, 152u * 4u), 256, 0, s>>>(a, n, b, b ? m : 0, flag);
-    BHUT_CUDA(cudaGetLastError());
-    note_launches(1);
-    return kOk;
-}
-
 int launch_normalize(const double* pts, int64_t n, int dim, const double* pmin, const double* pmax,
                      double top, double* out, cudaStream_t s)
 {

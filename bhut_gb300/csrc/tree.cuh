@@ -107,6 +107,42 @@ static __device__ __forceinline__ uint64_t quantise(double x, double pmin, doubl
     return q < 2097151ull ? q : 2097151ull;
 }
 
+// The same quantised coordinate with two FP64 operations instead of a
+// division: with y = RN(1/extent), q0 = RN(RN(x - pmin) * y) lies within
+// 3 * 2^-53 of RN(RN(x - pmin) / extent) (both are within that of the exact
+// quotient, which is at most 1), i.e. within 3 * 2^-32 in units of the
+// 2^-21 grid.  When q0 * 2^21 is at least 2^-29 away from every integer its
+// truncation is the reference's; otherwise (an exact grid point, a tiny
+// quotient: a few coordinates per build) the division is taken after all.
+// q0 * 2^21 is read from the bits of q0 (a power-of-two scaling is exact).
+// Only for offset == 0 (offset 0.5 marks a degenerate axis: exact path).
+static __device__ __forceinline__ uint64_t quantise_rcp(double x, double pmin, double extent,
+                                                        double rcp)
+{
+    const double a = __dsub_rn(x, pmin);
+    const uint64_t b = (uint64_t)__double_as_longlong(__dmul_rn(a, rcp));
+    if (b == 0) return 0;                            // a == 0: quotient exactly 0
+    const int e = (int)((b >> 52) & 0x7ff);
+    const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int s = 1054 - e;                          // fractional bits of q0 * 2^21
+    uint64_t k;
+    bool ok;
+    if ((b >> 63) || e == 0 || s < 1 || s > 80) {
+        k = 0;
+        ok = false;
+    } else if (s <= 52) {
+        k = m >> s;
+        const uint64_t frac = m & ((1ull << s) - 1);
+        const uint64_t thr = s > 29 ? (1ull << (s - 29)) : 1ull;
+        ok = frac >= thr && ((1ull << s) - frac) >= thr;
+    } else {                                         // q0 * 2^21 < 1
+        k = 0;
+        ok = s > 53 || m <= (1ull << 53) - (1ull << 25);
+    }
+    if (!ok) return quantise(x, pmin, extent, 0.0);
+    return k < 2097151ull ? k : 2097151ull;
+}
+
 static __device__ __forceinline__ uint64_t morton3(uint64_t cx, uint64_t cy, uint64_t cz)
 {
     return expand3(cx) | (expand3(cy) << 1) | (expand3(cz) << 2);
@@ -129,12 +165,19 @@ struct NodeOut {
 
 // Kernel launchers (build.cu, traverse.cu).
 // Bounding box: box[0..2] = min, box[3..5] = max, box[6] = max |mass| (0
-// without masses).  `partial` holds kBoxPartialDoubles doubles.
+// without masses), box[8..10] = RN(1 / (max - min)) per axis (1 for a zero
+// extent), box[11] = 1 if an axis has zero extent, box[12..14] = 1 if the
+// axis holds a NaN.  `partial` holds kBoxPartialDoubles doubles.
 constexpr unsigned kBoxMaxBlocks = 152u * 4u;
 constexpr int kBoxPartialDoubles = 8 * (int)kBoxMaxBlocks;
-constexpr int kBoxDoubles = 8;
+constexpr int kBoxDoubles = 16;
 int launch_bbox(const double* pos, const double* mass, int64_t n, int dim, double* partial,
                 unsigned* counter, double* box, unsigned* err, cudaStream_t s);
+// The same box while copying positions and masses to pos_copy / mass_copy
+// (either may be NULL); a non-finite value sets kErrNonFinite in *err.
+int launch_stage_bbox(const double* pos, const double* mass, int64_t n, int dim, double* pos_copy,
+                      double* mass_copy, double* partial, unsigned* counter, double* box,
+                      unsigned* err, cudaStream_t s);
 int launch_morton(const double* pos, int64_t n, int dim, const double* box, uint64_t* keys,
                   int32_t* idx, cudaStream_t s);
 int launch_gather(const double* pos, const double* mass, const int32_t* perm, int64_t n, int dim,
@@ -142,14 +185,23 @@ int launch_gather(const double* pos, const double* mass, const int32_t* perm, in
 int launch_topology(const TopoTables& tt, int32_t* first_child, int32_t* start, int32_t* count,
                     int32_t* parent, int32_t* leaf_list, unsigned* leaf_counter, unsigned* err,
                     cudaStream_t s);
+// Reorders the leaf list by first particle (siblings end up in neighbouring
+// entries, which the bottom-up pass merges inside a block).  `keys` holds
+// num_leaves entries; the scratch sort_scratch_bytes(num_leaves).
+int order_leaves(int32_t* leaf_list, int64_t num_leaves, const int32_t* start, uint64_t* keys,
+                 void* sort_scratch, cudaStream_t s);
+// Node boxes and moments from the leaves up (build, or refit with opos /
+// omass in input order); quadrupoles the same way.  `frontier` holds
+// num_leaves entries of scratch, `frontier_count` one counter.
 int launch_bottom_up(const TreeDev& t, const int32_t* leaf_list, int64_t num_leaves,
                      const int32_t* first_child, const int32_t* start, const int32_t* count,
                      const int32_t* parent, unsigned* arrive, NodeOut o, bool refit,
-                     const double* opos, const double* omass, unsigned* err, cudaStream_t s);
+                     const double* opos, const double* omass, int32_t* frontier,
+                     unsigned* frontier_count, unsigned* err, cudaStream_t s);
 int launch_quadrupoles(const TreeDev& t, const int32_t* leaf_list, int64_t num_leaves,
                        const int32_t* first_child, const int32_t* start, const int32_t* count,
-                       const int32_t* parent, unsigned* arrive, double* quad, unsigned* err,
-                       cudaStream_t s);
+                       const int32_t* parent, unsigned* arrive, double* quad, int32_t* frontier,
+                       unsigned* frontier_count, unsigned* err, cudaStream_t s);
 int launch_outside_root(const double* pos, int64_t n, int dim, const double* center0,
                         const double* half0, unsigned* flag, cudaStream_t s);
 int launch_traverse_exact(const TreeDev& t, const double* tx, const double* ty, const double* tz,
@@ -200,8 +252,6 @@ int launch_import_perm(const int64_t* in, int64_t n, int32_t* out, unsigned* err
 int launch_iota(int32_t* out, int64_t n, cudaStream_t s);
 int launch_widen_i32(const int32_t* in, int64_t n, int64_t* out, cudaStream_t s);
 int measure_fp32_peak(double* tflops);
-int launch_check_finite(const double* a, int64_t n, const double* b, int64_t m, unsigned* flag,
-                        cudaStream_t s);
 
 int direct_chunks(int64_t n, int64_t nt);
 int launch_direct(const double* pos, const double* mass, int64_t n, int dim, const double* targets,

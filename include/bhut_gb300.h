@@ -232,6 +232,11 @@ BHUT_API int bhut_batch_outside(const bhut_batch *b, const double *roots, uint8_
 
 BHUT_API void bhut_batch_destroy(bhut_batch *b);
 
+/* Device time of the traversal kernel of the last solve (CUDA events
+ * recorded around it, also inside a replayed graph), in milliseconds.  No
+ * counterpart in the reference; used for the roofline of the batched form. */
+BHUT_API int bhut_batch_traverse_ms(const bhut_batch *b, double *ms);
+
 /* Leapfrog update on device arrays (n, dim): v += kick * a, then, when
  * drift != 0, x += drift * v.  A kick-drift-kick step is
  * (kick = dt/2, drift = dt), a new acceleration, then (kick = dt/2, drift = 0). */
