@@ -11,7 +11,14 @@ per tick:
   optional cap on resident particles); a request that does not fit even on an
   empty server is rejected;
 * each tick: first half-kick and drift (``bhut_leapfrog``), one batched
-  solve of every resident system (``bhut_batch_*``), second half-kick;
+  solve (``bhut_batch_*``), second half-kick, for the systems that run this
+  tick.  With a per-solve particle budget (``solve_budget``) the running
+  systems are chosen shortest remaining work first (particles x remaining
+  steps), greedily up to the budget (at least one system), so small
+  requests do not wait for the largest resident system at every step;
+  the others keep their state in HBM and wait.  The choice is revisited at
+  every admission and retirement.  Without a budget every resident system
+  steps every tick;
 * each system refits its tree on its own schedule -- its Morton order is kept
   (``bhut_batch_keep_order``) and node boxes and moments are recomputed --
   and rebuilds it every ``rebuild_every`` of its own steps, or earlier when a
@@ -93,6 +100,51 @@ def retire_reason(steps_done: int, steps: int, waited: float, deadline: float | 
     return None
 
 
+def remaining_work(n: int, steps: int, steps_done: int, primed: bool) -> int:
+    """Particle-solves a request still needs: one per remaining step, plus
+    the initial force evaluation if it has not run yet."""
+    return n * (max(steps - steps_done, 0) + (0 if primed else 1))
+
+
+def choose_running(work: list[tuple[int, int, int]], budget: int | None) -> list[int]:
+    """Which resident systems step in the next solve.  ``work`` holds
+    (remaining work, particles, request id) per resident system; returns
+    positions in ``work``.  Without a budget: all of them.  With one:
+    shortest remaining work first (ties by request id), each system taken
+    while the running particle total stays within ``budget``; the first is
+    always taken, so a system larger than the budget still runs."""
+    if budget is None:
+        return list(range(len(work)))
+    order = sorted(range(len(work)), key=lambda k: (work[k][0], work[k][2]))
+    chosen, total = [], 0
+    for k in order:
+        n = work[k][1]
+        if chosen and total + n > budget:
+            continue
+        chosen.append(k)
+        total += n
+    return sorted(chosen)
+
+
+def size_class(n: int) -> str:
+    """Latency report classes by particle count."""
+    return "n<1e4" if n < 10_000 else ("1e4<=n<1e5" if n < 100_000 else "n>=1e5")
+
+
+def latency_summary(items: list[tuple[int, float]]) -> dict:
+    """p50/p99 latency overall and per size class from (particles,
+    latency) of finished requests."""
+    def stats(lat):
+        a = np.asarray(lat, dtype=float)
+        return {"count": int(a.size),
+                "p50_s": float(np.percentile(a, 50)) if a.size else None,
+                "p99_s": float(np.percentile(a, 99)) if a.size else None}
+    out = {"all": stats([t for _, t in items])}
+    for cls in ("n<1e4", "1e4<=n<1e5", "n>=1e5"):
+        out[cls] = stats([t for n, t in items if size_class(n) == cls])
+    return out
+
+
 def keeps_order(primed: bool, has_order: bool, steps_done: int, rebuild_every: int) -> bool:
     """Refit (keep the last Morton order) unless this system's rebuild is
     due: its first solve, and every ``rebuild_every`` of its own steps
@@ -167,7 +219,7 @@ class Server:
                  dt: float = 1e-3, rebuild_every: int = 10, form: str = "fp32",
                  criterion: str = "bh_offset", leaf_size: int = 16, targets_per_warp: int = 32,
                  hbm_budget: float = 150e9, max_active_particles: int | None = None,
-                 multipole: str = "quad"):
+                 multipole: str = "quad", solve_budget: int | None = None):
         import torch
         self.torch = torch
         self.theta, self.eps, self.G, self.dt = theta, softening, G, dt
@@ -175,6 +227,8 @@ class Server:
         self.leaf_size = leaf_size
         self.hbm_budget = hbm_budget
         self.max_active = max_active_particles
+        self.solve_budget = solve_budget
+        self.running: list[Request] = []   # the resident systems that step each tick
         self.L = _lib.load()
         self.stream = torch.cuda.current_stream().cuda_stream
         self.solver = BatchedSolver(dim=3, leaf_size=leaf_size, form=form, criterion=criterion,
@@ -228,13 +282,25 @@ class Server:
             r.forced_seen = int(forced[k])
 
     def _pack(self):
-        """Concatenates the resident systems' state into one set of device
-        arrays (after an admission or a retirement)."""
+        """Chooses the running systems and concatenates their state into one
+        set of device arrays (after an admission or a retirement).  Resident
+        systems that do not run keep a private copy of their state."""
         torch = self.torch
         self._sync_roots()
         dev = "cuda"
-        parts_x, parts_v, parts_a, parts_m = [], [], [], []
+        work = [(remaining_work(r.n, r.steps, r.steps_done, r.primed), r.n, r.rid)
+                for r in self.active]
+        self.running = [self.active[k] for k in choose_running(work, self.solve_budget)]
+        running = set(id(r) for r in self.running)
+        packed = set(id(r) for r in self.packed)
         for r in self.active:
+            if id(r) not in running and id(r) in packed:   # leaves the packed arrays
+                r.positions, r.velocities = r.positions.clone(), r.velocities.clone()
+                r.acc, r.masses = r.acc.clone(), r.masses.clone()
+                if r.order is not None:
+                    r.order = r.order.clone()
+        parts_x, parts_v, parts_a, parts_m = [], [], [], []
+        for r in self.running:
             parts_x.append(r.positions)
             parts_v.append(r.velocities)
             parts_a.append(r.acc)
@@ -243,31 +309,31 @@ class Server:
         self.v = torch.cat(parts_v).contiguous()
         self.a = torch.cat(parts_a).contiguous()
         self.m = torch.cat(parts_m).contiguous()
-        sizes = [r.n for r in self.active]
+        sizes = [r.n for r in self.running]
         self.off = np.zeros(len(sizes) + 1, dtype=np.int64)
         self.off[1:] = np.cumsum(sizes)
-        for k, r in enumerate(self.active):          # views into the packed arrays
+        for k, r in enumerate(self.running):         # views into the packed arrays
             s, e = int(self.off[k]), int(self.off[k + 1])
             r.positions, r.velocities, r.acc, r.masses = self.x[s:e], self.v[s:e], self.a[s:e], \
                 self.m[s:e]
             r.slot = (s, e)
         self.perm = torch.empty(int(self.off[-1]), dtype=torch.int32, device=dev)
-        self.packed = list(self.active)
+        self.packed = list(self.running)
         self._roots_dirty = True
-        self.peak_bytes = max(self.peak_bytes,
-                              float(self.off[-1]) * bytes_per_particle(self.leaf_size))
+        self.peak_bytes = max(self.peak_bytes, float(sum(r.n for r in self.active)) *
+                              bytes_per_particle(self.leaf_size))
 
     # -- one tick ------------------------------------------------------------
     def tick(self) -> None:
         torch = self.torch
         dt = self.dt
-        for r in self.active:                       # first half-kick + drift
+        for r in self.running:                       # first half-kick + drift
             if r.primed:
                 _leapfrog(self.L, r.positions, r.velocities, r.acc, r.n, 0.5 * dt, dt,
                           self.stream)
-        keep = np.zeros(len(self.active), dtype=np.uint8)
+        keep = np.zeros(len(self.running), dtype=np.uint8)
         perm_in = None
-        for k, r in enumerate(self.active):         # refit unless a rebuild is due
+        for k, r in enumerate(self.running):         # refit unless a rebuild is due
             if keeps_order(r.primed, r.order is not None, r.steps_done, self.rebuild_every):
                 keep[k] = 1
         self.solver.load(self.x, self.m, self.off)
@@ -276,8 +342,8 @@ class Server:
             # not kept anyway), forced-rebuild counters from zero.  Inside the
             # solve a kept system that has a particle beyond 1.1x its root box
             # is rebuilt (should_refit_vs_rebuild, bhut/tree/refit.py:236-249).
-            roots = np.zeros((len(self.active), 4))
-            for k, r in enumerate(self.active):
+            roots = np.zeros((len(self.running), 4))
+            for k, r in enumerate(self.running):
                 if r.root is not None:
                     roots[k] = r.root
                 r.forced_seen = 0
@@ -287,7 +353,7 @@ class Server:
             perm_in = torch.cat([
                 (r.order + int(self.off[k])) if r.order is not None
                 else torch.zeros(r.n, dtype=torch.int32, device="cuda")
-                for k, r in enumerate(self.active)])
+                for k, r in enumerate(self.running)])
             _lib.check(self.L.bhut_batch_keep_order(self.solver.h, keep.ctypes.data,
                                                     perm_in.data_ptr()))
         else:
@@ -299,7 +365,7 @@ class Server:
         ev1.record()
         self._solve_events.append((ev0, ev1))
         _lib.check(self.L.bhut_batch_order(self.solver.h, self.perm.data_ptr()))
-        for k, r in enumerate(self.active):
+        for k, r in enumerate(self.running):
             s, e = r.slot
             r.order = self.perm[s:e] - s
             if r.primed:                            # second half-kick
@@ -309,7 +375,7 @@ class Server:
             else:
                 r.primed = True                     # a(0): the initial force evaluation
             r.solves += 1
-        self.solves += len(self.active)
+        self.solves += len(self.running)
         self.accels += int(self.off[-1])
         self.ticks += 1
 
@@ -410,6 +476,7 @@ class Server:
         self._solve_events = []
         done = [r for r in self.finished if r.status == "done"]
         lat = np.array([r.latency for r in done if r.latency is not None])
+        by_class = latency_summary([(r.n, r.latency) for r in done if r.latency is not None])
         return {
             "requests_done": len(done),
             "requests_cancelled": sum(r.status == "cancelled" for r in self.finished),
@@ -420,6 +487,9 @@ class Server:
             "accels_per_s": self.accels / wall if wall else 0.0,
             "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else None,
             "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None,
+            "latency_by_size": by_class,
+            "requests_unfinished": len(self.active) + len(self.queue),
+            "solve_budget": self.solve_budget,
             "peak_resident_bytes_est": self.peak_bytes,
             "device_mem_used_peak_bytes": self.mem_peak,
             "device_mem_request_peak_bytes": self.mem_peak - self.mem_base,
@@ -482,26 +552,40 @@ class Server:
 
 def plain_path(requests: list[Request], *, theta: float = 0.5, softening: float = 0.01,
                G: float = 1.0, dt: float = 1e-3, rebuild_every: int = 10, form: str = "fast",
-               leaf_size: int = 32, realtime: bool = True, max_seconds: float | None = None) -> dict:
-    """The same stream, one request at a time through the public Tree API."""
+               leaf_size: int = 32, criterion: str = "bh", multipole: str = "mono",
+               realtime: bool = True, max_seconds: float | None = None,
+               order: str = "arrival") -> dict:
+    """The same stream, one request at a time through the public Tree API.
+    ``order``: "arrival" (first come, first served) or "shortest" (of the
+    requests that have arrived, the one with the least work next -- the
+    server's ordering, so that a comparison isolates batching and
+    residency).  Stops starting requests after ``max_seconds``."""
     import torch
-    queue = sorted(requests, key=lambda r: r.arrival)
+    pending = sorted(requests, key=lambda r: r.arrival)
     L = _lib.load()
     stream = torch.cuda.current_stream().cuda_stream
     t_start = time.perf_counter()
     solves = 0
     accels = 0
     done = []
-    for r in queue:
+    while pending:
         t = time.perf_counter() - t_start
         if max_seconds is not None and t > max_seconds:
             break
-        if realtime and r.arrival > t:
-            time.sleep(r.arrival - t)
+        arrived = [r for r in pending if r.arrival <= t or not realtime]
+        if not arrived:
+            time.sleep(max(0.0, pending[0].arrival - t))
+            continue
+        if order == "shortest":
+            r = min(arrived, key=lambda q: (q.n * q.steps, q.rid))
+        else:
+            r = arrived[0]
+        pending = [q for q in pending if q is not r]
         x = torch.as_tensor(np.asarray(r.positions), device="cuda").clone()
         v = torch.as_tensor(np.asarray(r.velocities), device="cuda").clone()
         m = torch.as_tensor(np.asarray(r.masses), device="cuda").clone()
-        tree = api.Tree(x, m, leaf_size=leaf_size, form=form).build()
+        tree = api.Tree(x, m, leaf_size=leaf_size, form=form, criterion=criterion,
+                        multipole=multipole).build()
         a = tree.accelerations(theta=theta, softening=softening, G=G)
         solves += 1
         for step in range(r.steps):
@@ -526,4 +610,8 @@ def plain_path(requests: list[Request], *, theta: float = 0.5, softening: float 
             "solves_per_s": solves / wall if wall else 0.0,
             "accels_per_s": accels / wall if wall else 0.0,
             "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else None,
-            "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None}
+            "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None,
+            "latency_by_size": latency_summary([(r.n, r.done_at - r.arrival) for r in done]),
+            "requests_unfinished": len(pending), "order": order,
+            "config": {"form": form, "theta": theta, "criterion": criterion,
+                       "multipole": multipole, "leaf_size": leaf_size}}

@@ -55,3 +55,35 @@ def test_retire_reasons():
     # cancellation wins over everything, completion over the deadline
     assert serve.retire_reason(10, 10, 9.0, 0.4, True) == "cancelled"
     assert serve.retire_reason(10, 10, 9.0, 0.4, False) == "done"
+
+
+def test_remaining_work_counts_the_initial_solve():
+    assert serve.remaining_work(1000, 100, 0, False) == 1000 * 101
+    assert serve.remaining_work(1000, 100, 0, True) == 1000 * 100
+    assert serve.remaining_work(1000, 100, 100, True) == 0
+
+
+def test_choose_running_shortest_work_first_within_budget():
+    # (remaining work, particles, request id)
+    work = [(5_000_000, 50_000, 0), (100_000, 1_000, 1), (900_000, 9_000, 2),
+            (2_000_000_000, 2_000_000, 3), (300_000, 3_000, 4)]
+    assert serve.choose_running(work, None) == [0, 1, 2, 3, 4]
+    # budget 13,000 particles: ids 1, 4, 2 fit (13,000), 0 does not, 3 does not
+    assert serve.choose_running(work, 13_000) == [1, 2, 4]
+    # the shortest job always runs, even when larger than the budget
+    assert serve.choose_running([(10**9, 2_000_000, 7)], 1000) == [0]
+    # a later, smaller system fills the budget that a larger one skipped
+    work2 = [(10, 10, 0), (20, 100, 1), (30, 5, 2)]
+    assert serve.choose_running(work2, 20) == [0, 2]
+    # ties broken by request id
+    assert serve.choose_running([(7, 1, 9), (7, 1, 2)], 1) == [1]
+
+
+def test_latency_summary_by_size_class():
+    items = [(5_000, 1.0), (8_000, 3.0), (50_000, 10.0), (2_000_000, 100.0)]
+    s = serve.latency_summary(items)
+    assert s["all"]["count"] == 4
+    assert s["n<1e4"]["count"] == 2 and s["n<1e4"]["p50_s"] == 2.0
+    assert s["1e4<=n<1e5"]["p99_s"] == 10.0
+    assert s["n>=1e5"]["count"] == 1
+    assert serve.latency_summary([])["all"]["p50_s"] is None
