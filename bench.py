@@ -8,6 +8,12 @@ inputs already resident in HBM.  ``e2e`` repeats the metric through the
 public API (``bhut_gb300.accelerations``) with host NumPy buffers, so the
 host<->device copies are inside its timed region.
 
+The same line carries bounded sub-records of the other named workloads:
+``exact`` (the IEEE-FP64 form at the headline workload), ``batched`` (2,048
+Plummer systems in one graph solve), ``precision`` (4M galaxy, FP32 form,
+three thetas) and ``served`` (200-request Poisson stream against the plain
+per-request path).
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--form exact|fast|fp32]
     python bench.py --impl reference ...   # the reference's algorithm on the host cores
 
@@ -246,14 +252,21 @@ def measure_gemm_peak(torch, dtype) -> float:
 # (error-free squares and sums), refined rsqrt and cube 11, m * w 4, three
 # float-float products and accumulations 36 -> 103 (plus one MUFU rsqrt;
 # the small-R range test and its selects are compiled out when the
-# softening bounds R from below, as in this workload).
+# softening bounds R from below, as in this workload).  The fp32 form's
+# counts live in bhut_gb300.reports.
 FF_OPS_PER_INTERACTION = 103
-# ... and of the fp32 form (fast.cuh): a pair term (pair_f32_partial:
-# displacement 9, r^2 + eps^2 3, cube 2, m * w 1, three FMAs into the leaf
-# partial 3 -> 18) and a monopole (pair_f32: the same 15 plus a Kahan step
-# per component 12 -> 27), each plus one MUFU rsqrt.
-F32_OPS_PER_PAIR = 18
-F32_OPS_PER_MONOPOLE = 27
+ARITH = {"exact": "IEEE FP64",
+         "fast": "float-float on the FP32 pipe (about 48-bit significand); FP64 bounding box, "
+                 "keys, centres of mass and rare fallbacks",
+         "fp32": "FP32 + Kahan; FP64 bounding box, keys and centres of mass"}
+DTYPE = {"exact": "f64", "fast": "f64-ff", "fp32": "f32"}
+# Algorithmic bytes of one rebuild (the build kernels' compulsory reads and
+# writes): per particle staging copy + box 64, Morton keys 36, digit
+# histograms 8, eight sort passes 8 x 24, Morton-ordered gather 68, leaf
+# moments 32; per node about 200 (moments, boxes, links of both children
+# read, its own written).
+BUILD_BYTES_PER_PARTICLE = 64 + 36 + 8 + 8 * 24 + 68 + 32
+BUILD_BYTES_PER_NODE = 200
 
 
 def run_ours(args, ws, rank, local):
@@ -315,7 +328,8 @@ def run_ours(args, ws, rank, local):
     t_max = _max_over_ranks(total_ms / 1e3, ws)
     value = ws * n * args.steps / t_max
 
-    # end to end through the public API with host buffers
+    # end to end through the public API with host buffers (one untimed call,
+    # then e2e_steps timed calls)
     e2e_steps = max(1, args.e2e_steps)
     bh.accelerations(pos, m, theta=THETA, softening=EPS, G=G, leaf_size=LEAF, form=args.form)
     torch.cuda.synchronize()
@@ -331,6 +345,7 @@ def run_ours(args, ws, rank, local):
     if rank != 0:
         h.close()
         return
+    hbm_peak = _measured_hbm_gbs()
     peak64 = measure_gemm_peak(torch, torch.float64)
     peak32 = measure_gemm_peak(torch, torch.float32)
     ffma = ctypes.c_double(0.0)
@@ -355,9 +370,10 @@ def run_ours(args, ws, rank, local):
             ops = FF_OPS_PER_INTERACTION * inter
             rule = f"{FF_OPS_PER_INTERACTION} FP32 ops per float-float pair or monopole term"
         else:
-            ops = F32_OPS_PER_PAIR * p2p + F32_OPS_PER_MONOPOLE * m2p
-            rule = (f"{F32_OPS_PER_PAIR} FP32 ops per pair term, {F32_OPS_PER_MONOPOLE} per "
-                    "Kahan-added monopole")
+            from bhut_gb300 import reports
+            ops = reports.fp32_ops(p2p, m2p, "mono")
+            rule = (f"{reports.F32_OPS_PER_PAIR} FP32 ops per pair term, "
+                    f"{reports.F32_OPS_PER_MONOPOLE} per Kahan-added monopole")
         achieved32 = ops / trav_s / 1e12
         # FP32 pipe lane-instructions per second (one FMA = 2 flop): the FMA
         # chains of bhut_measure_fp32_peak, and cuBLAS SGEMM for comparison
@@ -379,24 +395,52 @@ def run_ours(args, ws, rank, local):
                                 "frac": achieved64 / peak64,
                                 "rule": f"{FLOPS_PER_INTERACTION} flop per interaction vs "
                                         "measured DGEMM"}}
+    build_s = (total_ms - trav_ms) / args.steps / 1e3
+    m_nodes = h.info()[1]
+    build_bytes = BUILD_BYTES_PER_PARTICLE * n + BUILD_BYTES_PER_NODE * m_nodes
     line = {
         "metric": METRIC, "value": value, "unit": "accels/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": DTYPE[args.form], "arith": ARITH[args.form],
         "data": "synthetic", "config": _workload_desc(n, args.form),
         "e2e": {"value": e2e_value, "unit": "accels/s",
                 "h2d_bytes_per_step": int(pos.nbytes + m.nbytes),
-                "d2h_bytes_per_step": int(n * 3 * 8), "api": "bhut_gb300.accelerations"},
+                "d2h_bytes_per_step": int(n * 3 * 8), "api": "bhut_gb300.accelerations",
+                "timed_calls": e2e_steps, "untimed_calls_before": 1},
         "gpu_launches": int(launches),
         "roofline": roofline,
         "traversal_ms": trav_s * 1e3,
-        "build_ms": (total_ms - trav_ms) / args.steps,
+        "build_ms": build_s * 1e3,
+        "roofline_build": {"bound": "hbm", "achieved": build_bytes / build_s / 1e9,
+                           "peak": hbm_peak, "unit": "GB/s",
+                           "frac": build_bytes / build_s / 1e9 / hbm_peak,
+                           "bytes_per_rebuild": int(build_bytes),
+                           "bytes_rule": f"{BUILD_BYTES_PER_PARTICLE} B per particle + "
+                                         f"{BUILD_BYTES_PER_NODE} B per node (compulsory "
+                                         "reads and writes of the build kernels)",
+                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)",
+                           "note": "build_ms is the device time from the start of the "
+                                   "rebuild call to the start of the traversal, host "
+                                   "round trips (input check, error word) included"},
         "interactions_per_solve": {"p2p": p2p, "m2p": m2p, "node_visits": visits,
                                    "fp64_fallback_decisions": fb_dec, "fp64_pairs": fb_pairs},
         "clocks": clk,
     }
-    if ws == 1 and not args.no_served:
-        line["served"] = served_summary(args)
+    if ws == 1 and not args.quick:
+        from bhut_gb300 import reports
+        fma_rate = ffma_tflops / 2.0
+        if not args.no_exact:
+            line["exact"] = reports.exact_record(pos_d, m_d, theta=THETA, eps=EPS, G=G,
+                                                 leaf=LEAF, fp64_peak=peak64)
+        if not args.no_batched:
+            line["batched"] = reports.batched_record(fma_rate=fma_rate)
+        if not args.no_precision:
+            line["precision"] = reports.precision_record(fma_rate=fma_rate)
+        if not args.no_served:
+            line["served"] = reports.served_record(
+                count=args.served_count, server_seconds=args.served_seconds,
+                plain_seconds=args.served_seconds, fast_seconds=args.served_fast_seconds)
     if not args.no_cpu_baseline:
         cb = cpu_solve_sample(pos, m, args.cpu_sample)
         line["cpu_baseline"] = {
@@ -409,28 +453,14 @@ def run_ours(args, ws, rank, local):
     print(json.dumps(line), flush=True)
 
 
-def served_summary(args) -> dict:
-    """The served half of the metric: the continuous-batching server against
-    the plain per-request GPU path on the same Poisson stream (24 systems,
-    N log-uniform in [1e3, 2e6], 100 KDK steps each, 200 requests/s), with
-    both configurations' median error vs FP64 direct sum."""
-    from bhut_gb300 import reports
-    r = reports.served_report(count=args.served_count, plain_seconds=args.served_plain_seconds,
-                              closed_loop=False, emit=False)
-    sv, pl = r["served"], r["plain"]
-    return {
-        "workload": f"{r['requests']} requests, {r['particles']:,} particles, Poisson "
-                    f"{r['rate_per_s']:.0f}/s, {r['steps']} KDK steps each, refit every step, "
-                    "rebuild every 10",
-        "served_config": r["served_config"], "plain_config": r["plain_config"],
-        "solves_per_s": sv["solves_per_s"], "latency_p50_s": sv["latency_p50_s"],
-        "latency_p99_s": sv["latency_p99_s"], "plain_solves_per_s": pl["solves_per_s"],
-        "plain_latency_p50_s": pl["latency_p50_s"], "plain_latency_p99_s": pl["latency_p99_s"],
-        "plain_requests_done": pl["requests_done"],
-        "solves_per_s_ratio": r["solves_per_s_ratio"],
-        "median_err_vs_fp64_direct": {"served": r["median_err_vs_direct"]["served"],
-                                      "plain": r["median_err_vs_direct"]["plain"]},
-    }
+def _measured_hbm_gbs() -> float:
+    """HBM copy bandwidth measured on this machine (MEASURED_PEAKS.json), else
+    the stated fallback."""
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return 6800.0
 
 
 def _traffic_from_profile(args):
@@ -452,14 +482,22 @@ def main():
     ap.add_argument("--form", choices=["exact", "fast", "fp32"], default=None)
     ap.add_argument("--n", "--particles", dest="n", type=int, default=N_DEFAULT,
                     help="particles (--particles under torchrun, whose parser takes --n)")
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--ref-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="headline only: no exact, batched, precision or served sub-record")
+    ap.add_argument("--no-exact", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--no-served", action="store_true",
-                    help="skip the served-stream comparison (about a minute)")
-    ap.add_argument("--served-count", type=int, default=24)
-    ap.add_argument("--served-plain-seconds", type=float, default=60.0)
+                    help="skip the served-stream comparison (about two minutes)")
+    ap.add_argument("--served-count", type=int, default=200)
+    ap.add_argument("--served-seconds", type=float, default=45.0,
+                    help="wall-time cap of the server and of the plain same-config leg")
+    ap.add_argument("--served-fast-seconds", type=float, default=20.0,
+                    help="wall-time cap of the plain FP64-accurate leg")
     args = ap.parse_args()
     if args.form is None:
         from bhut_gb300.api import DEFAULT_FORM

@@ -315,6 +315,285 @@ def scaling_report(sizes=(100_000, 1_000_000, 4_000_000, 16_000_000, 64_000_000)
     return lines
 
 
+# ---------------------------------------------------------------------------
+# Sub-records of the benchmark line (bench.py): each bounded in time
+# ---------------------------------------------------------------------------
+# FP32-pipe operations per evaluation, counted from bhut_gb300/csrc/fast.cuh:
+# a pair term into a leaf partial (pair_f32_partial: displacement 9,
+# r^2 + eps^2 3, cube 2, m * w 1, three FMAs 3), a Kahan-added monopole
+# (pair_f32: the same 15 plus a Kahan step per component 12), a Kahan-added
+# monopole + quadrupole node (node_quad_f32: displacement 9, r^2 3, powers 3,
+# Q d 9, d.Q d 3, force factor 4, per component 6 -> 49), each plus one MUFU
+# rsqrt.
+F32_OPS_PER_PAIR = 18
+F32_OPS_PER_MONOPOLE = 27
+F32_OPS_PER_QUAD_NODE = 49
+
+
+def fp32_ops(p2p: int, m2p: int, multipole: str) -> int:
+    node = F32_OPS_PER_QUAD_NODE if multipole == "quad" else F32_OPS_PER_MONOPOLE
+    return F32_OPS_PER_PAIR * p2p + node * m2p
+
+
+def fp32_roofline(ops: int, seconds: float, fma_rate: float, kernel: str, multipole: str) -> dict:
+    """Achieved FP32-pipe operations per second of a traversal against the
+    FP32 FMA lane rate measured in the same run (T ops/s)."""
+    achieved = ops / seconds / 1e12
+    node = F32_OPS_PER_QUAD_NODE if multipole == "quad" else F32_OPS_PER_MONOPOLE
+    return {"bound": "fp32", "kernel": kernel, "achieved": achieved, "peak": fma_rate,
+            "unit": "T FP32-pipe ops/s", "frac": achieved / fma_rate,
+            "work_per_launch": int(ops),
+            "work_rule": f"{F32_OPS_PER_PAIR} FP32 ops per pair term, {node} per "
+                         f"{'monopole+quadrupole' if multipole == 'quad' else 'monopole'} node, "
+                         "x evaluations counted by the kernel",
+            "peak_source": "independent FP32 FMA chains on every SM, measured in this run"}
+
+
+def exact_record(pos_d, m_d, *, theta: float, eps: float, G: float, leaf: int,
+                 fp64_peak: float) -> dict:
+    """The IEEE-FP64 form (form "exact") at the headline workload: one
+    rebuild + traversal, device time by CUDA events on the handle's stream."""
+    import torch
+    from .api import _Handle
+    n = int(pos_d.shape[0])
+    stream = torch.cuda.Stream()
+    h = _Handle(3, leaf, stream=stream.cuda_stream)
+    h.set_form("exact")
+    out = torch.empty_like(pos_d)
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record(stream)
+    h.rebuild(pos_d, m_d)
+    e1.record(stream)
+    h.accel_self(theta, eps, G, out)
+    e2.record(stream)
+    e2.synchronize()
+    trav = e1.elapsed_time(e2) / 1e3
+    total = e0.elapsed_time(e2) / 1e3
+    p2p, m2p, visits = h.stats()
+    h.close()
+    flops = 20 * (p2p + m2p)
+    achieved = flops / trav / 1e12
+    return {"form": "exact", "arith": "IEEE FP64", "dtype": "f64", "accels_per_s": n / total,
+            "solve_ms": total * 1e3, "traversal_ms": trav * 1e3,
+            "roofline": {"bound": "fp64", "kernel": "k_traverse_exact", "achieved": achieved,
+                         "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                         "work_rule": "20 flop x (pair + monopole evaluations counted by the "
+                                      "kernel)",
+                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"},
+            "interactions_per_solve": {"p2p": p2p, "m2p": m2p, "node_visits": visits}}
+
+
+def batched_record(*, nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: int = 11,
+                   theta: float = 0.5, eps: float = 0.01, G: float = 1.0,
+                   multipole: str = "quad", reps: int = 3, plain_sample: int = 64,
+                   err_systems: int = 16, fma_rate: float | None = None) -> dict:
+    """The batched form on its named workload: ``nsys`` Plummer spheres in one
+    CUDA-graph solve (FP32 form, autotuned leaf / targets per warp / stack),
+    systems/s and accels/s, error against FP64 direct sums, the plain
+    per-system path on a sample, and the roofline of k_batch_traverse."""
+    import torch
+    from . import batch
+    systems = workloads.plummer_batch(nsys, nmin, nmax, seed=seed)
+    pos, m, off = batch.concat_systems(systems)
+    ntot = int(off[-1])
+    pd = torch.as_tensor(pos).cuda()
+    md = torch.as_tensor(m).cuda()
+    t0 = time.perf_counter()
+    cfg, times = batch.autotune(pd, md, off, theta=theta, softening=eps, G=G, form="fp32",
+                                multipole=multipole, repeats=1)
+    t_tune = time.perf_counter() - t0
+    sv = batch.BatchedSolver(leaf_size=cfg["leaf_size"], form="fp32",
+                             targets_per_warp=cfg["targets_per_warp"], use_graph=True,
+                             multipole=multipole, stack=cfg["stack"])
+    sv.load(pd, md, off)
+    out = torch.empty_like(pd)
+    sv.solve(theta=theta, softening=eps, G=G, out=out)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    trav = []
+    ev0.record()
+    for _ in range(reps):
+        sv.solve(theta=theta, softening=eps, G=G, out=out)
+        trav.append(sv.traverse_ms() / 1e3)
+    ev1.record()
+    ev1.synchronize()
+    t_batch = ev0.elapsed_time(ev1) / 1e3 / reps
+    p2p, m2p, _ = sv.stats()
+    acc = out.cpu().numpy()
+    sv.close()
+    rng = np.random.default_rng(seed + 1)
+    pick = rng.choice(nsys, min(plain_sample, nsys), replace=False)
+    t_plain = 0.0
+    for s in pick:
+        p_, m_ = systems[s]
+        tr = api.Tree(p_, m_, leaf_size=32, form="fast").build()
+        tr.accelerations(theta=theta, softening=eps, G=G)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        tr.rebuild(p_, m_)
+        tr.accelerations(theta=theta, softening=eps, G=G)
+        torch.cuda.synchronize()
+        t_plain += time.perf_counter() - t1
+        tr.close()
+    plain_sps = len(pick) / t_plain
+    errs = []
+    for s in rng.choice(nsys, min(err_systems, nsys), replace=False):
+        p_, m_ = systems[s]
+        ref = np.asarray(api.direct_accelerations(p_, m_, softening=eps, G=G))
+        errs.append(precision.error_distribution(acc[off[s]:off[s + 1]], ref))
+    t_trav = float(np.median(trav))
+    rec = {
+        "workload": f"{nsys} Plummer spheres, N log-uniform in [{nmin}, {nmax}] "
+                    f"({ntot:,} particles), a ~ U[0.5, 2], own seeds, equal masses 1/N",
+        "theta": theta, "softening": eps, "form": "fp32", "arith": "FP32 + Kahan; FP64 keys, "
+        "centres of mass and quadrupoles", "criterion": "bh", "multipole": multipole,
+        "config": cfg, "autotune_s": t_tune, "cuda_graph": True,
+        "solve_ms": t_batch * 1e3, "traversal_ms": t_trav * 1e3,
+        "systems_per_s": nsys / t_batch, "accels_per_s": ntot / t_batch,
+        "interactions": {"p2p": p2p, "m2p": m2p},
+        "plain_per_system": {"form": "fast", "systems_timed": int(len(pick)),
+                             "systems_per_s": plain_sps},
+        "speedup_vs_plain_systems_per_s": (nsys / t_batch) / plain_sps,
+        "err_vs_fp64_direct": {"systems": len(errs),
+                               "median_of_medians": float(np.median([e["median"] for e in errs])),
+                               "worst_p99": float(max(e["p99"] for e in errs))},
+    }
+    if fma_rate:
+        rec["roofline"] = fp32_roofline(fp32_ops(p2p, m2p, multipole), t_trav, fma_rate,
+                                        "k_batch_traverse", multipole)
+    return rec
+
+
+def precision_record(*, n: int = 4_000_000, n_sample: int = 8192, thetas=(0.3, 0.5, 0.7),
+                     eps: float = 0.005, G: float = 1.0, seed: int = 7,
+                     fma_rate: float | None = None) -> dict:
+    """The precision form on its named workload (galaxy disc + bulge):
+    per theta an autotuned leaf size, FP32/Kahan accels/s with the roofline of
+    k_traverse_fp32, its error distribution against the FP64 direct sum on
+    sampled targets and against the FP64-accurate form on all targets."""
+    import torch
+    from .api import _Handle
+    pos, m = workloads.galaxy(n, seed=seed)
+    idx = precision.sample_indices(n, n_sample, seed=seed + 1)
+    ref = precision.direct_reference(pos, m, idx, softening=eps, G=G)
+    pd = torch.as_tensor(pos).cuda()
+    md = torch.as_tensor(m).cuda()
+    out = torch.empty_like(pd)
+    stream = torch.cuda.Stream()
+    rows = []
+    for theta in thetas:
+        leaf, times = precision.autotune_leaf_size(pd, md, theta=theta, softening=eps, G=G,
+                                                   form="fp32", repeats=1)
+        h = _Handle(3, leaf, stream=stream.cuda_stream)
+        h.set_form("fp32")
+        h.rebuild(pd, md)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        h.rebuild(pd, md)
+        e1.record(stream)
+        h.accel_self(theta, eps, G, out)
+        e2.record(stream)
+        e2.synchronize()
+        trav = e1.elapsed_time(e2) / 1e3
+        total = e0.elapsed_time(e2) / 1e3
+        p2p, m2p, _ = h.stats()
+        a32 = out.cpu().numpy()
+        h.set_form("fast")
+        h.accel_self(theta, eps, G, out)
+        a64 = out.cpu().numpy()
+        h.close()
+        row = {"theta": theta, "leaf_size": leaf,
+               "autotune_s": {str(k): v for k, v in times.items()},
+               "accels_per_s": n / total, "solve_ms": total * 1e3, "traversal_ms": trav * 1e3,
+               "err_vs_fp64_direct": precision.error_distribution(a32[idx], ref),
+               "err_vs_fp64_form_fast": precision.error_distribution(a32, a64),
+               "fast_err_vs_fp64_direct": precision.error_distribution(a64[idx], ref),
+               "interactions": {"p2p": p2p, "m2p": m2p}}
+        if fma_rate:
+            row["roofline"] = fp32_roofline(fp32_ops(p2p, m2p, "mono"), trav, fma_rate,
+                                            "k_traverse_fp32", "mono")
+        rows.append(row)
+    return {"workload": f"galaxy N={n:,}: 70% exponential disc (Rd 3.0, sech^2 z0 0.3), 30% "
+                        "Hernquist bulge (a 0.5), equal masses", "softening": eps,
+            "form": "fp32", "arith": "FP32 + Kahan; FP64 bbox, keys and centres of mass",
+            "multipole": "mono", "sampled_targets": int(len(idx)), "by_theta": rows}
+
+
+def served_record(*, count: int = 200, rate: float = 200.0, steps: int = 100, seed: int = 21,
+                  server_seconds: float = 45.0, plain_seconds: float = 45.0,
+                  fast_seconds: float = 20.0, solve_budget: int = 2_000_000,
+                  theta: float = 0.7, criterion: str = "bh_offset", multipole: str = "quad",
+                  leaf: int = 16, fast_theta: float = 0.33, err_requests: int = 6,
+                  hbm_budget: float = 150e9) -> dict:
+    """The served form on its named stream (Poisson ``rate``/s, N log-uniform
+    in [1e3, 2e6], half Plummer half cubes, ``steps`` KDK steps, refit every
+    step, rebuild every 10, HBM budget 150 GB), each leg bounded in wall
+    time: the continuous-batching server (shortest remaining work first
+    within a per-solve particle budget) against the plain per-request path
+    with the same form, theta, criterion, multipole and leaf size (the same
+    arithmetic per system, so equal error by construction) and the same
+    ordering, and against the plain FP64-accurate path (form fast) at a
+    theta whose error vs FP64 direct sum is close to the server's."""
+    import dataclasses
+    from . import serve
+    base = serve.request_stream(count, rate=rate, steps=steps, seed=seed)
+    fresh = lambda: [dataclasses.replace(r) for r in base]  # noqa: E731
+    total_n = sum(r.n for r in base)
+    by_size = sorted(base, key=lambda r: r.n)
+    pick = [by_size[int(round(k))] for k in np.linspace(0, len(by_size) - 1, err_requests)]
+    e_srv, e_fast, e_fast05 = [], [], []
+    for r in pick:
+        idx = precision.sample_indices(r.n, 2048, seed=1)
+        ref = precision.direct_reference(r.positions, r.masses, idx, softening=0.01)
+        a_s = api.accelerations(r.positions, r.masses, theta=theta, softening=0.01, form="fp32",
+                                criterion=criterion, multipole=multipole, leaf_size=leaf)
+        a_f = api.accelerations(r.positions, r.masses, theta=fast_theta, softening=0.01,
+                                form="fast")
+        a_5 = api.accelerations(r.positions, r.masses, theta=0.5, softening=0.01, form="fast")
+        e_srv.append(precision.error_distribution(a_s[idx], ref)["median"])
+        e_fast.append(precision.error_distribution(a_f[idx], ref)["median"])
+        e_fast05.append(precision.error_distribution(a_5[idx], ref)["median"])
+    kw = dict(theta=theta, softening=0.01, dt=1e-3, rebuild_every=10, form="fp32",
+              criterion=criterion, multipole=multipole, leaf_size=leaf)
+    wp, wm = workloads.plummer(4096, seed=5)
+    warm = [serve.Request(-1 - k, 0.0, wp, np.zeros_like(wp), wm, steps=12) for k in range(2)]
+    sv = serve.Server(**kw)
+    sv.run(warm, realtime=False)
+    sv.close()
+    sv = serve.Server(**kw, hbm_budget=hbm_budget, solve_budget=solve_budget)
+    st = sv.run(fresh(), realtime=True, max_seconds=server_seconds)
+    sv.close()
+    pl = serve.plain_path(fresh(), realtime=True, max_seconds=plain_seconds, order="shortest",
+                          **kw)
+    pf = serve.plain_path(fresh(), realtime=True, max_seconds=fast_seconds, order="shortest",
+                          theta=fast_theta, softening=0.01, dt=1e-3, rebuild_every=10,
+                          form="fast", leaf_size=32)
+    ratio = lambda a, b: a / b if b else None  # noqa: E731
+    return {
+        "workload": f"{count} requests ({total_n:,} particles), Poisson {rate:.0f}/s, N "
+                    f"log-uniform in [1e3, 2e6], half Plummer half uniform cubes, {steps} KDK "
+                    "steps each (dt 1e-3, eps 0.01), refit every step, rebuild every 10, HBM "
+                    f"budget {hbm_budget / 1e9:.0f} GB",
+        "server_config": {"form": "fp32", "theta": theta, "criterion": criterion,
+                          "multipole": multipole, "leaf_size": leaf,
+                          "scheduling": "shortest remaining work first",
+                          "solve_budget_particles": solve_budget},
+        "wall_caps_s": {"server": server_seconds, "plain_same_config": plain_seconds,
+                        "plain_fast": fast_seconds},
+        "server": st,
+        "plain_same_config": pl,
+        "plain_fast_equal_error": pf,
+        "solves_per_s_ratio_vs_same_config": ratio(st["solves_per_s"], pl["solves_per_s"]),
+        "accels_per_s_ratio_vs_same_config": ratio(st["accels_per_s"], pl["accels_per_s"]),
+        "solves_per_s_ratio_vs_fast": ratio(st["solves_per_s"], pf["solves_per_s"]),
+        "median_err_vs_fp64_direct": {
+            "server_and_plain_same_config": float(np.median(e_srv)),
+            f"plain_fast_theta_{fast_theta}": float(np.median(e_fast)),
+            "plain_fast_theta_0.5": float(np.median(e_fast05)),
+            "requests_n": [r.n for r in pick]},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("report", choices=["precision", "batched", "served", "scaling"])
