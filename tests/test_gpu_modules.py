@@ -107,3 +107,27 @@ def test_targets_and_statistics_modules(golden_small, oracle_mod):
         ot = oracle_mod.build_tree(pos, m, 4)
         nodes, parts, monos = oracle_mod.tree_statistics(ot, pos, 0.5)
         assert st["total_operations"] == parts + monos
+
+
+def test_aabb_infinities_nan_and_signed_zero_like_numpy():
+    """aabb (bbox.py:14-46) on values the integer-image min/max must order
+    like numpy: infinities, NaN (propagates to its axis) and signed zeros."""
+    rng = np.random.default_rng(13)
+    pts = rng.standard_normal((5000, 3))
+    pts[17, 0] = np.inf
+    pts[4000, 0] = -np.inf
+    pts[123, 1] = np.nan
+    pts[:, 2] = np.where(rng.random(5000) < 0.5, 0.0, -0.0)
+    lo, hi = aabb(pts)
+    with np.errstate(invalid="ignore"):
+        ref_lo, ref_hi = pts.min(0), pts.max(0)
+    assert lo[0] == -np.inf and hi[0] == np.inf
+    assert np.isnan(lo[1]) and np.isnan(hi[1])
+    assert lo[2] == 0.0 and hi[2] == 0.0   # -0.0 == 0.0, as numpy's
+    np.testing.assert_array_equal(lo, ref_lo)
+    np.testing.assert_array_equal(hi, ref_hi)
+    # finite inputs in 1-D and 2-D: exact extrema
+    for d in (1, 2):
+        q = rng.standard_normal((3001, d)) * 1e3
+        lo, hi = aabb(q)
+        assert np.array_equal(lo, q.min(0)) and np.array_equal(hi, q.max(0))
