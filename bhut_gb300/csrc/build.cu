@@ -143,23 +143,47 @@ k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t 
     }
     __syncthreads();
     if (!s_last) return;
-    // last block: reduce the partials (ordered images; |mass| bits)
+    // last block: reduce the partials (ordered images; |mass| bits), all
+    // threads striding over the blocks, then across the block
     __threadfence();
-    if (tid < 7) {
-        const bool is_lo = tid < 3, is_m = tid == 6;
-        const int d = tid < 3 ? tid : tid - 3;
-        if (is_m || d < dim) {
-            uint64_t acc = is_lo ? ~0ull : 0ull;
-            for (unsigned g = 0; g < gridDim.x; g++) {
-                const uint64_t k = (uint64_t)__double_as_longlong(__ldcg(&partial[g * 8 + tid]));
-                if (is_lo) acc = k < acc ? k : acc;
-                else acc = k > acc ? k : acc;
-            }
-            box[tid] = is_m ? __longlong_as_double((long long)acc)
-                            : __longlong_as_double((long long)ord_inv(acc));
-        } else {
-            box[tid] = tid < 3 ? INFINITY : -INFINITY;
+    uint64_t a[7];
+    for (int k = 0; k < 3; k++) { a[k] = ~0ull; a[3 + k] = 0ull; }
+    a[6] = 0ull;
+    unsigned nanmask = 0;
+    for (unsigned g = tid; g < gridDim.x; g += kBoxThreads) {
+        for (int k = 0; k < 7; k++) {
+            const uint64_t v = (uint64_t)__double_as_longlong(__ldcg(&partial[g * 8 + k]));
+            if (k < 3) a[k] = v < a[k] ? v : a[k];
+            else a[k] = v > a[k] ? v : a[k];
         }
+        nanmask |= (unsigned)__ldcg(&partial[g * 8 + 7]);
+    }
+    constexpr int kBoxWarps = kBoxThreads / 32;
+    __shared__ uint64_t s_red[7][kBoxWarps];
+    for (int k = 0; k < 7; k++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint64_t v = __shfl_down_sync(0xffffffffu, a[k], o);
+            if (k < 3) a[k] = v < a[k] ? v : a[k];
+            else a[k] = v > a[k] ? v : a[k];
+        }
+        if ((tid & 31) == 0) s_red[k][tid >> 5] = a[k];
+    }
+    if (nanmask) atomicOr(&s_nan, nanmask << 4);   // bits 4..6: the grid's NaN axes
+    __syncthreads();
+    if (tid < 7) {
+        uint64_t acc = s_red[tid][0];
+        for (int w = 1; w < kBoxWarps; w++) {
+            const uint64_t v = s_red[tid][w];
+            if (tid < 3) acc = v < acc ? v : acc;
+            else acc = v > acc ? v : acc;
+        }
+        const int d = tid < 3 ? tid : tid - 3;
+        if (tid == 6)
+            box[6] = __longlong_as_double((long long)acc);
+        else if (d < dim)
+            box[tid] = __longlong_as_double((long long)ord_inv(acc));
+        else
+            box[tid] = tid < 3 ? INFINITY : -INFINITY;
     }
     __syncthreads();
     // per axis the reciprocal of the extent that the Morton quantiser uses
@@ -177,9 +201,7 @@ k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t 
             box[8 + d] = r;
         }
         box[11] = degenerate ? 1.0 : 0.0;
-        unsigned nanmask = 0;
-        for (unsigned g = 0; g < gridDim.x; g++) nanmask |= (unsigned)__ldcg(&partial[g * 8 + 7]);
-        for (int d = 0; d < 3; d++) box[12 + d] = (nanmask >> d) & 1u ? 1.0 : 0.0;
+        for (int d = 0; d < 3; d++) box[12 + d] = (s_nan >> (4 + d)) & 1u ? 1.0 : 0.0;
         *done_counter = 0;
     }
 }
@@ -576,10 +598,14 @@ k_bottom_up(Ops ops, TreeDev t, const int32_t* __restrict__ leaf_list, int64_t n
 // The rest of the tree, from the frontier nodes up, by one block: each
 // climb step is taken by the second child to arrive at a parent (arrival
 // counters).  All climbers run in this block, so block-scope fences order
-// a child's writes before its arrival.  A climb longer than kMaxClimb
-// (parent links with a cycle, possible in an imported TreeData) stops with
-// an error instead of looping.
+// a child's writes before its arrival, and while the frontier is small the
+// counters live in a shared-memory hash table keyed by node id (a frontier
+// of f nodes has f - 1 ancestors to count at most); a larger frontier
+// counts in global memory.  A climb longer than kMaxClimb (parent links
+// with a cycle, possible in an imported TreeData) stops with an error
+// instead of looping.
 constexpr int kBuTopThreads = 1024;
+constexpr int kBuTopHash = 4096;   // shared counters: frontiers of up to 2048 nodes
 
 template <class Ops>
 __global__ void __launch_bounds__(kBuTopThreads)
@@ -589,7 +615,15 @@ k_bottom_up_top(Ops ops, TreeDev t, const int32_t* __restrict__ first_child,
                 const unsigned* __restrict__ frontier_count, int64_t cap,
                 unsigned* __restrict__ err)
 {
+    __shared__ int32_t s_key[kBuTopHash];
+    __shared__ unsigned s_cnt[kBuTopHash];
     const unsigned nf = min(*frontier_count, (unsigned)cap);
+    const bool shared_counters = nf <= kBuTopHash / 2;
+    for (int i = threadIdx.x; i < kBuTopHash; i += blockDim.x) {
+        s_key[i] = -1;
+        s_cnt[i] = 0;
+    }
+    __syncthreads();
     for (unsigned f = threadIdx.x; f < nf; f += blockDim.x) {
         int32_t node = frontier[f];
         for (int step = 0;; step++) {
@@ -598,7 +632,22 @@ k_bottom_up_top(Ops ops, TreeDev t, const int32_t* __restrict__ first_child,
             if (p < 0) break;
             if (bad_parent(t, first_child, p)) { atomicOr(err, kErrBadNode); break; }
             __threadfence_block();
-            const unsigned prev = atomicAdd_block(&arrive[p], 1u);
+            unsigned prev;
+            if (shared_counters) {
+                // linear probing from a multiplicative hash; at most f - 1
+                // keys in 2f slots, so a free or matching slot is found
+                unsigned h = ((unsigned)p * 2654435761u) >> 20;   // 12 bits
+                int probes = 0;
+                for (;; h = (h + 1) & (kBuTopHash - 1)) {
+                    const int32_t k = atomicCAS(&s_key[h], -1, p);
+                    if (k == -1 || k == p) break;
+                    if (++probes >= kBuTopHash) break;
+                }
+                if (probes >= kBuTopHash) { atomicOr(err, kErrBadNode); break; }
+                prev = atomicAdd(&s_cnt[h], 1u);
+            } else {
+                prev = atomicAdd_block(&arrive[p], 1u);
+            }
             if (prev == 0) break;
             __threadfence_block();
             ops.internal(p, first_child[p]);

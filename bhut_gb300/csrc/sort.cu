@@ -158,7 +158,7 @@ k_sort_scan(uint32_t* __restrict__ counts, int64_t tiles, const uint32_t* __rest
 
 // k_sort_scatter: see the file comment.  `next_counts` (may be null) gets
 // the digit at `next_shift` of every key, per destination tile.
-__global__ void __launch_bounds__(kSortThreads)
+__global__ void __launch_bounds__(kSortThreads, 3)
 k_sort_scatter(const uint64_t* __restrict__ keys_in, const int32_t* __restrict__ vals_in,
                uint64_t* __restrict__ keys_out, int32_t* __restrict__ vals_out, int64_t n,
                int shift, const uint32_t* __restrict__ offsets, int64_t tiles,
@@ -175,7 +175,6 @@ k_sort_scatter(const uint64_t* __restrict__ keys_in, const int32_t* __restrict__
     __syncthreads();
 
     uint64_t k[kItems];
-    int32_t v[kItems];
     uint32_t rank[kItems];
     const unsigned lt_mask = (1u << lane) - 1u;
 #pragma unroll
@@ -183,7 +182,6 @@ k_sort_scatter(const uint64_t* __restrict__ keys_in, const int32_t* __restrict__
         const int64_t p = item_pos(tile, warp, i, lane);
         const bool valid = p < n;
         k[i] = valid ? keys_in[p] : ~0ull;
-        v[i] = valid ? vals_in[p] : 0;
         const unsigned d = (unsigned)(k[i] >> shift) & 0xFFu;
         // lanes holding the same digit (warp multi-split by eight ballots)
         unsigned peers = __ballot_sync(FULL, valid);
@@ -222,7 +220,7 @@ k_sort_scatter(const uint64_t* __restrict__ keys_in, const int32_t* __restrict__
             const uint32_t lpos = sm.local_off[d] + sm.warp_counts[warp][d] + rank[i];
             if (lpos < (uint32_t)kSortTile) {   // always true; guards shared memory
                 sm.keys[lpos] = k[i];
-                sm.vals[lpos] = v[i];
+                sm.vals[lpos] = vals_in[p];    // (read here: fewer live registers)
             }
         }
     }
@@ -290,6 +288,11 @@ int radix_sort_pairs(uint64_t* keys, int32_t* vals, int64_t n, int bits, void* s
             BHUT_CUDA(cudaFuncSetAttribute(k_sort_scatter,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)sizeof(ScatterSmem)));
+            // all of the unified L1/shared storage as shared memory: three
+            // 59 KB tiles per SM
+            BHUT_CUDA(cudaFuncSetAttribute(k_sort_scatter,
+                                           cudaFuncAttributePreferredSharedMemoryCarveout,
+                                           (int)cudaSharedmemCarveoutMaxShared));
             if (dev >= 0 && dev < 64) smem_set[dev].store(true, std::memory_order_release);
         }
     }
