@@ -504,12 +504,14 @@ __device__ void internal_node(int32_t id, int32_t fc, int dim, bool refit, NodeO
 
 // Leaves are taken in groups of kBuThreads consecutive entries of the leaf
 // list (one thread each).  Inside the group the lowest kBuLevels levels are
-// merged in shared memory: threads i and i ^ 2^j holding the two children of
-// one node pair up and the lower one computes the parent (the block barrier
-// orders the children's writes; no atomics, no device-wide fences).  A
-// thread left without a partner -- its sibling is in another group, or the
-// tree is irregular there -- hands its node to the frontier list, from
-// which k_bottom_up_top finishes the tree.
+// merged in shared memory: at level j slot k holds the node covering leaves
+// [k 2^j, (k+1) 2^j) of the group; thread t < slots / 2 pairs slots 2t and
+// 2t + 1 and, when they are the two children of one node, computes that node
+// into slot t (compacted, so the FP64 work of a level runs on as few warps
+// as possible; block barriers order the children's writes; no atomics, no
+// device-wide fences).  A node whose sibling is not in its pair -- it lies
+// in another group, or the tree is irregular there -- goes to the frontier
+// list, from which k_bottom_up_top finishes the tree.
 constexpr int kBuThreads = 256;
 constexpr int kBuLevels = 8;   // log2(kBuThreads)
 static_assert((1 << kBuLevels) == kBuThreads, "group size is 2^kBuLevels");
@@ -517,6 +519,14 @@ static_assert((1 << kBuLevels) == kBuThreads, "group size is 2^kBuLevels");
 __device__ __forceinline__ bool bad_parent(const TreeDev& t, const int32_t* first_child, int32_t p)
 {
     return p >= t.m || (p >= 0 && (first_child[p] < 1 || first_child[p] + 1 >= t.m));
+}
+
+__device__ __forceinline__ void hand_over(int32_t node, int32_t* frontier, unsigned* frontier_count,
+                                          int64_t cap, unsigned* err)
+{
+    const unsigned k = atomicAdd(frontier_count, 1u);
+    if (k < (unsigned)cap) frontier[k] = node;
+    else atomicOr(err, kErrBadNode);
 }
 
 // Node operations of a bottom-up pass: the moments (build and refit modes)
@@ -541,8 +551,7 @@ k_bottom_up(Ops ops, TreeDev t, const int32_t* __restrict__ leaf_list, int64_t n
             int32_t* __restrict__ frontier, unsigned* __restrict__ frontier_count,
             unsigned* __restrict__ err)
 {
-    __shared__ int32_t s_par[kBuThreads];
-    __shared__ int s_alive[kBuThreads];
+    __shared__ int32_t s_node[kBuThreads];
     const int tid = threadIdx.x;
     for (int64_t base = (int64_t)blockIdx.x * kBuThreads; base < num_leaves;
          base += (int64_t)gridDim.x * kBuThreads) {
@@ -555,43 +564,39 @@ k_bottom_up(Ops ops, TreeDev t, const int32_t* __restrict__ leaf_list, int64_t n
             alive = false;
         }
         if (alive) ops.leaf(id);
-        int32_t node = id;
-        bool hand_over = false;
-        for (int j = 0; j < kBuLevels; j++) {
-            int32_t p = -1;
-            if (alive) {
-                p = parent[node];
-                if (bad_parent(t, first_child, p)) {
-                    atomicOr(err, kErrBadNode);
-                    alive = false;
-                    p = -1;
+        s_node[tid] = alive ? id : -1;
+        __syncthreads();
+        for (int j = 0, slots = kBuThreads; j < kBuLevels; j++, slots >>= 1) {
+            int32_t out = -1;
+            if (tid < slots / 2) {
+                const int32_t a = s_node[2 * tid], b = s_node[2 * tid + 1];
+                int32_t pa = -1, pb = -1;
+                if (a >= 0) {
+                    pa = parent[a];
+                    if (bad_parent(t, first_child, pa)) { atomicOr(err, kErrBadNode); pa = -2; }
                 }
-            }
-            s_par[tid] = p;
-            s_alive[tid] = alive;
-            __syncthreads();
-            const int partner = tid ^ (1 << j);
-            const bool pair = alive && s_alive[partner] && p >= 0 && s_par[partner] == p;
-            if (alive && !pair) {   // the parent is completed elsewhere (or this is the root)
-                hand_over = p >= 0;
-                alive = false;
-            }
-            if (pair) {
-                if ((tid >> j) & 1) {
-                    alive = false;
-                } else {
-                    ops.internal(p, first_child[p]);
-                    node = p;
+                if (b >= 0) {
+                    pb = parent[b];
+                    if (bad_parent(t, first_child, pb)) { atomicOr(err, kErrBadNode); pb = -2; }
+                }
+                if (pa >= 0 && pa == pb) {
+                    ops.internal(pa, first_child[pa]);
+                    out = pa;
+                } else {   // parents completed elsewhere (or roots: nothing to do)
+                    if (pa >= 0) hand_over(a, frontier, frontier_count, num_leaves, err);
+                    if (pb >= 0) hand_over(b, frontier, frontier_count, num_leaves, err);
                 }
             }
             __syncthreads();
+            if (tid < slots / 2) s_node[tid] = out;
+            __syncthreads();
         }
-        if (alive) hand_over = parent[node] >= 0;
-        if (hand_over) {
-            const unsigned k = atomicAdd(frontier_count, 1u);
-            if (k < (unsigned)num_leaves) frontier[k] = node;
-            else atomicOr(err, kErrBadNode);
+        if (tid == 0 && s_node[0] >= 0) {
+            const int32_t p = parent[s_node[0]];
+            if (bad_parent(t, first_child, p)) atomicOr(err, kErrBadNode);
+            else if (p >= 0) hand_over(s_node[0], frontier, frontier_count, num_leaves, err);
         }
+        __syncthreads();
     }
 }
 
