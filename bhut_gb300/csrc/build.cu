@@ -209,7 +209,8 @@ k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t 
 // ---------------------------------------------------------------------------
 // K2: Morton keys (input order) and the identity payload for the sort.
 // ---------------------------------------------------------------------------
-__global__ void k_morton(const double* __restrict__ pos, int64_t n, int dim,
+template <int dim>
+__global__ void k_morton(const double* __restrict__ pos, int64_t n,
                          const double* __restrict__ box, uint64_t* __restrict__ keys,
                          int32_t* __restrict__ idx)
 {
@@ -378,7 +379,10 @@ __device__ double pairwise_sum(F load, int64_t n)
 // One leaf: tight AABB (build only), pairwise mass, row-order weighted sum.
 // In refit mode positions come from the caller's original-order arrays via
 // perm (refit.py:133-149); in build mode from the sorted SoA.
-__device__ void leaf_node(int32_t id, int dim, bool refit, const TreeDev& t,
+// DIM is a template parameter so that the per-axis accumulators stay in
+// registers (a runtime axis index would place them in local memory).
+template <int DIM>
+__device__ void leaf_node(int32_t id, bool refit, const TreeDev& t,
                           const double* __restrict__ opos, const double* __restrict__ omass,
                           const int32_t* __restrict__ start, const int32_t* __restrict__ count,
                           NodeOut o)
@@ -397,7 +401,7 @@ __device__ void leaf_node(int32_t id, int dim, bool refit, const TreeDev& t,
 #pragma unroll 4
         for (int64_t i = 0; i < c; i++) {
             const double mi = t.sm[s + i];
-            for (int d = 0; d < dim; d++) {
+            for (int d = 0; d < DIM; d++) {
                 const double v = axes[d][s + i];
                 const uint64_t k = ord_key((uint64_t)__double_as_longlong(v));
                 klo[d] = k < klo[d] ? k : klo[d];
@@ -406,15 +410,15 @@ __device__ void leaf_node(int32_t id, int dim, bool refit, const TreeDev& t,
             }
         }
         double lo[3], hi[3];
-        for (int d = 0; d < dim; d++) {
+        for (int d = 0; d < DIM; d++) {
             lo[d] = __longlong_as_double((long long)ord_inv(klo[d]));
             hi[d] = __longlong_as_double((long long)ord_inv(khi[d]));
         }
         double ext = 0.0;
-        for (int d = 0; d < dim; d++) {
+        for (int d = 0; d < DIM; d++) {
             o.lo[3 * id + d] = lo[d];
             o.hi[3 * id + d] = hi[d];
-            o.center[dim * id + d] = __dmul_rn(__dadd_rn(lo[d], hi[d]), 0.5);
+            o.center[DIM * id + d] = __dmul_rn(__dadd_rn(lo[d], hi[d]), 0.5);
             double e = __dsub_rn(hi[d], lo[d]);
             ext = (d == 0 || e > ext) ? e : ext;
         }
@@ -427,17 +431,17 @@ __device__ void leaf_node(int32_t id, int dim, bool refit, const TreeDev& t,
         for (int64_t i = 0; i < c; i++) {
             int64_t p = t.perm[s + i];
             double mi = omass[p];
-            for (int d = 0; d < dim; d++)
-                acc[d] = __dadd_rn(acc[d], __dmul_rn(mi, opos[p * dim + d]));
+            for (int d = 0; d < DIM; d++)
+                acc[d] = __dadd_rn(acc[d], __dmul_rn(mi, opos[p * DIM + d]));
         }
     }
     NodeCM cm;
     double com[3];
     for (int d = 0; d < 3; d++) com[d] = 0.0;
     if (total > 0) {
-        for (int d = 0; d < dim; d++) com[d] = __ddiv_rn(acc[d], total);
+        for (int d = 0; d < DIM; d++) com[d] = __ddiv_rn(acc[d], total);
     } else {
-        for (int d = 0; d < dim; d++) com[d] = o.center[dim * id + d];
+        for (int d = 0; d < DIM; d++) com[d] = o.center[DIM * id + d];
     }
     cm.x = com[0]; cm.y = com[1]; cm.z = com[2]; cm.w = total;
     o.cm[id] = cm;
@@ -453,13 +457,14 @@ __device__ __forceinline__ NodeCM load_cm_cg(const NodeCM* p)
     return NodeCM{u.x, u.y, v.x, v.y};
 }
 
-__device__ void internal_node(int32_t id, int32_t fc, int dim, bool refit, NodeOut o)
+template <int DIM>
+__device__ void internal_node(int32_t id, int32_t fc, bool refit, NodeOut o)
 {
     NodeCM a = load_cm_cg(&o.cm[fc]);
     NodeCM b = load_cm_cg(&o.cm[fc + 1]);
     if (!refit) {
         double ext = 0.0;
-        for (int d = 0; d < dim; d++) {
+        for (int d = 0; d < DIM; d++) {
             const uint64_t l0 = ord_key((uint64_t)__double_as_longlong(__ldcg(&o.lo[3 * fc + d])));
             const uint64_t l1 = ord_key((uint64_t)__double_as_longlong(__ldcg(&o.lo[3 * (fc + 1) + d])));
             const uint64_t h0 = ord_key((uint64_t)__double_as_longlong(__ldcg(&o.hi[3 * fc + d])));
@@ -468,7 +473,7 @@ __device__ void internal_node(int32_t id, int32_t fc, int dim, bool refit, NodeO
             const double hi = __longlong_as_double((long long)ord_inv(h1 > h0 ? h1 : h0));
             o.lo[3 * id + d] = lo;
             o.hi[3 * id + d] = hi;
-            o.center[dim * id + d] = __dmul_rn(__dadd_rn(lo, hi), 0.5);
+            o.center[DIM * id + d] = __dmul_rn(__dadd_rn(lo, hi), 0.5);
             double e = __dsub_rn(hi, lo);
             ext = (d == 0 || e > ext) ? e : ext;
         }
@@ -480,24 +485,24 @@ __device__ void internal_node(int32_t id, int32_t fc, int dim, bool refit, NodeO
     double total, w[3] = {0.0, 0.0, 0.0};
     if (!refit) {
         total = __dadd_rn(0.0, __dadd_rn(__dadd_rn(-0.0, ma), mb));
-        for (int d = 0; d < dim; d++)
+        for (int d = 0; d < DIM; d++)
             w[d] = __dadd_rn(__dadd_rn(w[d], __dmul_rn(ma, ca[d])), __dmul_rn(mb, cb[d]));
     } else {
         total = 0.0;
         if (ma > 0) {
             total = __dadd_rn(total, ma);
-            for (int d = 0; d < dim; d++) w[d] = __dadd_rn(w[d], __dmul_rn(ma, ca[d]));
+            for (int d = 0; d < DIM; d++) w[d] = __dadd_rn(w[d], __dmul_rn(ma, ca[d]));
         }
         if (mb > 0) {
             total = __dadd_rn(total, mb);
-            for (int d = 0; d < dim; d++) w[d] = __dadd_rn(w[d], __dmul_rn(mb, cb[d]));
+            for (int d = 0; d < DIM; d++) w[d] = __dadd_rn(w[d], __dmul_rn(mb, cb[d]));
         }
     }
     double com[3] = {0.0, 0.0, 0.0};
     if (total > 0) {
-        for (int d = 0; d < dim; d++) com[d] = __ddiv_rn(w[d], total);
+        for (int d = 0; d < DIM; d++) com[d] = __ddiv_rn(w[d], total);
     } else {
-        for (int d = 0; d < dim; d++) com[d] = o.center[dim * id + d];
+        for (int d = 0; d < DIM; d++) com[d] = o.center[DIM * id + d];
     }
     o.cm[id] = NodeCM{com[0], com[1], com[2], total};
 }
@@ -512,9 +517,11 @@ __device__ void internal_node(int32_t id, int32_t fc, int dim, bool refit, NodeO
 // device-wide fences).  A node whose sibling is not in its pair -- it lies
 // in another group, or the tree is irregular there -- goes to the frontier
 // list, from which k_bottom_up_top finishes the tree.
-constexpr int kBuThreads = 256;
-constexpr int kBuLevels = 8;   // log2(kBuThreads)
-static_assert((1 << kBuLevels) == kBuThreads, "group size is 2^kBuLevels");
+#ifndef BHUT_BU_LEVELS
+#define BHUT_BU_LEVELS 8   // tuning: leaves per group = 2^levels
+#endif
+constexpr int kBuLevels = BHUT_BU_LEVELS;
+constexpr int kBuThreads = 1 << kBuLevels;
 
 __device__ __forceinline__ bool bad_parent(const TreeDev& t, const int32_t* first_child, int32_t p)
 {
@@ -531,6 +538,7 @@ __device__ __forceinline__ void hand_over(int32_t node, int32_t* frontier, unsig
 
 // Node operations of a bottom-up pass: the moments (build and refit modes)
 // or the quadrupoles.
+template <int DIM>
 struct MomentOps {
     TreeDev t;
     NodeOut o;
@@ -539,8 +547,8 @@ struct MomentOps {
     const double* omass;
     const int32_t* start;
     const int32_t* count;
-    __device__ void leaf(int32_t id) const { leaf_node(id, t.dim, refit, t, opos, omass, start, count, o); }
-    __device__ void internal(int32_t p, int32_t fc) const { internal_node(p, fc, t.dim, refit, o); }
+    __device__ void leaf(int32_t id) const { leaf_node<DIM>(id, refit, t, opos, omass, start, count, o); }
+    __device__ void internal(int32_t p, int32_t fc) const { internal_node<DIM>(p, fc, refit, o); }
 };
 
 template <class Ops>
@@ -820,7 +828,8 @@ int launch_stage_bbox(const double* pos, const double* mass, int64_t n, int dim,
 int launch_morton(const double* pos, int64_t n, int dim, const double* box, uint64_t* keys,
                   int32_t* idx, cudaStream_t s)
 {
-    k_morton<<<grid_for(n, 256), 256, 0, s>>>(pos, n, dim, box, keys, idx);
+    if (dim == 3) k_morton<3><<<grid_for(n, 256), 256, 0, s>>>(pos, n, box, keys, idx);
+    else k_morton<2><<<grid_for(n, 256), 256, 0, s>>>(pos, n, box, keys, idx);
     BHUT_CUDA(cudaGetLastError());
     note_launches(1);
     return kOk;
@@ -862,7 +871,11 @@ int launch_bottom_up(const TreeDev& t, const int32_t* leaf_list, int64_t num_lea
                      const double* opos, const double* omass, int32_t* frontier,
                      unsigned* frontier_count, unsigned* err, cudaStream_t s)
 {
-    return launch_climb(MomentOps{t, o, refit, opos, omass, start, count}, t, leaf_list,
+    if (t.dim == 3)
+        return launch_climb(MomentOps<3>{t, o, refit, opos, omass, start, count}, t, leaf_list,
+                            num_leaves, first_child, start, count, parent, arrive, frontier,
+                            frontier_count, err, s);
+    return launch_climb(MomentOps<2>{t, o, refit, opos, omass, start, count}, t, leaf_list,
                         num_leaves, first_child, start, count, parent, arrive, frontier,
                         frontier_count, err, s);
 }
