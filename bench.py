@@ -9,6 +9,7 @@ public API (``bhut_gb300.accelerations``) with host NumPy buffers, so the
 host<->device copies are inside its timed region.
 
 The same line carries bounded sub-records of the other named workloads:
+``c1`` (10,000 Gaussian particles, the reference's CPU-runnable case),
 ``exact`` (the IEEE-FP64 form at the headline workload), ``batched`` (2,048
 Plummer systems in one graph solve), ``precision`` (4M galaxy, FP32 form,
 three thetas) and ``served`` (200-request Poisson stream against the plain
@@ -178,6 +179,23 @@ def cpu_solve_sample(pos, m, sample_targets: int, seed: int = 0) -> dict:
             "sample_targets": len(idx), "cores": threads}
 
 
+def cpu_solve_all(pos, m, acc_gpu) -> dict:
+    """The oracle's full solve (serial build, traversal of every target on
+    all host threads) of a small workload, timed; with the relative L2
+    difference of the GPU result from it."""
+    from oracle import oracle
+    threads = host_threads()
+    t0 = time.perf_counter()
+    tree = oracle.build_tree(pos, m, LEAF)
+    ref = oracle.accelerations(tree, pos, m, theta=THETA, softening=EPS, G=G, nthreads=threads)
+    t = time.perf_counter() - t0
+    rel = float(np.linalg.norm(acc_gpu - ref) / np.linalg.norm(ref))
+    return {"value": len(pos) / t, "unit": "accels/s", "cores": threads, "kind": "port",
+            "sample": f"oracle (C restatement of the reference's path): full solve of all "
+                      f"{len(pos):,} targets, {t:.3f} s",
+            "gpu_rel_l2_vs_oracle": rel}
+
+
 def run_reference(args, ws, rank):
     """--impl reference: the reference's algorithm (oracle port, C, OpenMP on
     every host core) on the same workload; rank 0 only."""
@@ -246,15 +264,19 @@ def measure_gemm_peak(torch, dtype) -> float:
     return 2.0 * n ** 3 / best / 1e12
 
 
-# FP32-pipe operations of one float-float pair (or monopole) term of the fast
-# form, counted from bhut_gb300/csrc/fast.cuh (pair_ff, 3-D, target inside
-# the box): displacement 15 (5 per axis), r^2 + eps^2 and its low part 37
-# (error-free squares and sums), refined rsqrt and cube 11, m * w 4, three
-# float-float products and accumulations 36 -> 103 (plus one MUFU rsqrt;
-# the small-R range test and its selects are compiled out when the
-# softening bounds R from below, as in this workload).  The fp32 form's
-# counts live in bhut_gb300.reports.
-FF_OPS_PER_INTERACTION = 103
+# Instructions of one float-float pair (or monopole) term of the fast form,
+# counted from bhut_gb300/csrc/fast.cuh (pair_ff_soft, 3-D, target inside
+# the box, softening bounding R from below as in this workload): exact
+# displacement and squares 21, cross term and r^2 low part 4, three
+# non-negative FastTwoSums into r^2 21 (6 of them min/max on the ALU pipe),
+# MUFU rsqrt 1, refinement and cube 10, three float-float products and
+# magnitude-ordered two-sum accumulations 36 (9 compare/select on the ALU
+# pipe) -> 93 for a leaf pair in the unit-mass frame (every particle the same
+# mass), 97 with the mass product (monopoles, or unequal masses).  Of these,
+# 77 / 81 run on the FP32 (FMA) pipe.  The fp32 form's counts live in
+# bhut_gb300.reports.
+FF_INSTR_UNIT_PAIR, FF_INSTR_MASS_PAIR = 93, 97
+FF_FMA_UNIT_PAIR, FF_FMA_MASS_PAIR = 77, 81
 ARITH = {"exact": "IEEE FP64",
          "fast": "float-float on the FP32 pipe (about 48-bit significand); FP64 bounding box, "
                  "keys, centres of mass and rare fallbacks",
@@ -367,8 +389,15 @@ def run_ours(args, ws, rank, local):
                          "by the kernel)"}
     else:
         if args.form == "fast":
-            ops = FF_OPS_PER_INTERACTION * inter
-            rule = f"{FF_OPS_PER_INTERACTION} FP32 ops per float-float pair or monopole term"
+            unit = bool(m[0] > 0 and np.all(m == m[0]))
+            ipair = FF_INSTR_UNIT_PAIR if unit else FF_INSTR_MASS_PAIR
+            fpair = FF_FMA_UNIT_PAIR if unit else FF_FMA_MASS_PAIR
+            ops = ipair * p2p + FF_INSTR_MASS_PAIR * m2p
+            fma_ops = fpair * p2p + FF_FMA_MASS_PAIR * m2p
+            rule = (f"{ipair} pair-term instructions per leaf pair{' (unit-mass frame)' if unit else ''}"
+                    f", {FF_INSTR_MASS_PAIR} per monopole (FP32 + ALU + MUFU; one warp "
+                    "instruction per clock per SM sub-partition is both the issue limit and "
+                    "the FFMA rate below)")
         else:
             from bhut_gb300 import reports
             ops = reports.fp32_ops(p2p, m2p, "mono")
@@ -383,7 +412,9 @@ def run_ours(args, ws, rank, local):
             "bound": "fp32",
             "kernel": "k_traverse_fast" if args.form == "fast" else "k_traverse_fp32",
             "achieved": achieved32,
-            "peak": fma_rate, "unit": "T FP32-pipe ops/s", "frac": achieved32 / fma_rate,
+            "peak": fma_rate,
+            "unit": "T instr/s" if args.form == "fast" else "T FP32-pipe ops/s",
+            "frac": achieved32 / fma_rate,
             "traffic": traffic,
             "peak_source": "independent FP32 FMA chains on every SM, measured in this run "
                            "(bhut_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
@@ -391,6 +422,10 @@ def run_ours(args, ws, rank, local):
             "peak_sgemm_source": "cuBLAS SGEMM 4096^3 (TF32 off) measured in this run, / 2",
             "work_per_launch": ops,
             "work_rule": f"{rule} x evaluations counted by the kernel",
+            **({"fp32_pipe_frac": fma_ops / trav_s / 1e12 / fma_rate,
+                "fp32_pipe_rule": f"{fpair} FP32-pipe ops per leaf pair, {FF_FMA_MASS_PAIR} per "
+                                  "monopole, against the same FFMA rate"}
+               if args.form == "fast" else {}),
             "fp64_equivalent": {"achieved": achieved64, "peak": peak64, "unit": "TFLOP/s",
                                 "frac": achieved64 / peak64,
                                 "rule": f"{FLOPS_PER_INTERACTION} flop per interaction vs "
@@ -427,9 +462,13 @@ def run_ours(args, ws, rank, local):
                                    "fp64_fallback_decisions": fb_dec, "fp64_pairs": fb_pairs},
         "clocks": clk,
     }
+    c1 = None
     if ws == 1 and not args.quick:
         from bhut_gb300 import reports
         fma_rate = ffma_tflops / 2.0
+        if not args.no_c1:
+            c1 = reports.c1_record(fma_rate=fma_rate)
+            line["c1"] = c1[0]
         if not args.no_exact:
             line["exact"] = reports.exact_record(pos_d, m_d, theta=THETA, eps=EPS, G=G,
                                                  leaf=LEAF, fp64_peak=peak64)
@@ -449,6 +488,8 @@ def run_ours(args, ws, rank, local):
                       f"N={n:,} ({cb['t_build_s']:.2f} s) + traversal of "
                       f"{cb['sample_targets']} random targets ({cb['t_sample_s']:.2f} s, "
                       f"{cb['cores']} threads), extrapolated to N targets"}
+        if c1 is not None:
+            line["c1"]["cpu_baseline"] = cpu_solve_all(*c1[2], c1[1])
     h.close()
     print(json.dumps(line), flush=True)
 
@@ -489,6 +530,8 @@ def main():
     ap.add_argument("--quick", action="store_true",
                     help="headline only: no exact, batched, precision or served sub-record")
     ap.add_argument("--no-exact", action="store_true")
+    ap.add_argument("--no-c1", action="store_true",
+                    help="skip the 10,000-particle Gaussian sub-record")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--no-served", action="store_true",

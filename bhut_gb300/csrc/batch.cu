@@ -49,7 +49,8 @@ k_seg_bbox(const double* __restrict__ pos, const double* __restrict__ mass,
     const int64_t p0 = off[s], p1 = off[s + 1];
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     double mm = 0.0;
-    bool bad = false;
+    bool bad = false, mdiff = false;
+    const double m0 = p1 > p0 ? mass[p0] : 0.0;
     for (int64_t i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
         for (int d = 0; d < dim; d++) {
             const double v = pos[i * dim + d];
@@ -59,6 +60,7 @@ k_seg_bbox(const double* __restrict__ pos, const double* __restrict__ mass,
         }
         const double am = fabs(mass[i]);
         bad |= !isfinite(am);
+        mdiff |= __double_as_longlong(mass[i]) != __double_as_longlong(m0);
         mm = am > mm ? am : mm;
     }
     __shared__ double red[kSegThreads / 32][7];
@@ -78,7 +80,8 @@ k_seg_bbox(const double* __restrict__ pos, const double* __restrict__ mass,
         for (int d = 0; d < 3; d++) { red[warp][d] = lo[d]; red[warp][3 + d] = hi[d]; }
         red[warp][6] = mm;
     }
-    __syncthreads();
+    // every mass of the system bit-equal to the first (unit-mass frame)
+    const bool uniform = !__syncthreads_or(mdiff);
     if (threadIdx.x == 0) {
         for (int w = 1; w < kSegThreads / 32; w++) {
             for (int d = 0; d < 3; d++) {
@@ -89,6 +92,7 @@ k_seg_bbox(const double* __restrict__ pos, const double* __restrict__ mass,
         }
         for (int d = 0; d < 3; d++) { box[s * 8 + d] = lo[d]; box[s * 8 + 3 + d] = hi[d]; }
         box[s * 8 + 6] = mm;
+        box[s * 8 + 7] = uniform && m0 > 0.0 && isfinite(m0) ? 1.0 : 0.0;
     }
 }
 
@@ -335,6 +339,7 @@ k_seg_frames(TreeDev t, const int64_t* __restrict__ part_off, const int64_t* __r
     __shared__ FastFrame f;
     if (threadIdx.x == 0) {
         frame_from_box(box + s * 8, dim, &f);
+        frame_unit_mass(box[s * 8 + 6], box[s * 8 + 7] != 0.0, &f);
         frames[s] = f;
     }
     __syncthreads();
@@ -344,7 +349,8 @@ k_seg_frames(TreeDev t, const int64_t* __restrict__ part_off, const int64_t* __r
         split_grid(__dmul_rn(__dsub_rn(t.sy[i], f.c[1]), f.s), h.y, l.y);
         if (dim == 3) split_grid(__dmul_rn(__dsub_rn(t.sz[i], f.c[2]), f.s), h.z, l.z);
         else h.z = l.z = 0.0f;
-        split_plain(__dmul_rn(t.sm[i], f.ms), h.w, l.w);
+        if (f.unit) { h.w = 1.0f; l.w = 0.0f; }   // every mass is m0: exactly 1 in units of m0
+        else split_plain(__dmul_rn(t.sm[i], f.ms), h.w, l.w);
         ph[i] = h;
         pl[i] = l;
     }
@@ -580,8 +586,8 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                             unsigned fb = 0;   // pairs left to FP64, taken after the loop
                             if (soft) {
                                 for (int q = sub; q < cn; q += LPT)
-                                    pair_ff<DIM, false, false>(Th, Tl, sh[w][q], sl[w][q], e2h,
-                                                               e2l, ah, al);
+                                    pair_ff_soft<DIM, false>(Th, Tl, sh[w][q], sl[w][q], e2h, e2l,
+                                                             ah, al);
                             } else {
                                 for (int q = sub; q < cn; q += LPT)
                                     fb |= (unsigned)!pair_ff<DIM, false>(Th, Tl, sh[w][q],
@@ -648,6 +654,8 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                                                ah, al);
                         else
                             pair_f32<DIM>(Th, Tl, nhv, nlv, e2h, ah, al);
+                    } else if (soft) {
+                        pair_ff_soft<DIM, false>(Th, Tl, nhv, nlv, e2h, e2l, ah, al);
                     } else if (!pair_ff<DIM, false>(Th, Tl, nhv, nlv, e2h, e2l, ah, al)) {
                         const NodeCM cm = t.cm[node];
                         pair_fp64<DIM>(x, y, z, cm.x, cm.y, cm.z, cm.w, eps2, a64);
@@ -935,6 +943,20 @@ int bits_for(int64_t v)
 
 // All device work of one solve (build + traversal), stream-ordered, no host
 // synchronisation: this is what a CUDA graph captures.
+// Records a timing event on s.  Under stream capture a plain record only
+// marks a dependency and the event is never recorded when the graph runs;
+// an external record becomes a graph node that records it on every replay.
+int record_timing_event(cudaEvent_t e, cudaStream_t s)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    BHUT_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs == cudaStreamCaptureStatusActive)
+        BHUT_CUDA(cudaEventRecordWithFlags(e, s, cudaEventRecordExternal));
+    else
+        BHUT_CUDA(cudaEventRecord(e, s));
+    return kOk;
+}
+
 int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out)
 {
     cudaStream_t s = b->stream;
@@ -1021,7 +1043,7 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
                 eps, G, b->mac, out, b->err.as<unsigned>(), b->stats.as<unsigned long long>()};
     const bool fp32 = b->form == BHUT_FORM_FP32;
     const int stk = b->stack;
-    if (b->ev_trav[0]) BHUT_CUDA(cudaEventRecord(b->ev_trav[0], s));
+    if (b->ev_trav[0]) BHUT_TRY(record_timing_event(b->ev_trav[0], s));
     if (dim == 3) {
         if (fp32 && b->tpw == 32) launch_batch_traverse<3, true, 32>(stk, s, bd, a);
         else if (fp32) launch_batch_traverse<3, true, 16>(stk, s, bd, a);
@@ -1032,7 +1054,7 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
         else launch_batch_traverse<2, false, 32>(stk, s, bd, a);
     }
     BHUT_CUDA(cudaGetLastError());
-    if (b->ev_trav[1]) BHUT_CUDA(cudaEventRecord(b->ev_trav[1], s));
+    if (b->ev_trav[1]) BHUT_TRY(record_timing_event(b->ev_trav[1], s));
     note_launches(1);
     return kOk;
 }

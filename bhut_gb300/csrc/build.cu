@@ -87,8 +87,10 @@ k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t 
         }
     }
     uint64_t mm = 0ull;   // |mass| bits: non-negative doubles order as integers
+    bool mdiff = false;   // a mass differs from mass[0] (bit for bit)
     if (mass) {
         const uint64_t* __restrict__ q = reinterpret_cast<const uint64_t*>(mass);
+        const uint64_t m0b = __ldg(q);
         uint64_t* __restrict__ qc = reinterpret_cast<uint64_t*>(mass_copy);
         for (int64_t i0 = first; i0 < n; i0 += kBoxBatch * stride) {
             uint64_t b[kBoxBatch];
@@ -105,6 +107,7 @@ k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t 
                     bad |= !finite_bits(b[u]);
                     const uint64_t a = b[u] & 0x7FFFFFFFFFFFFFFFull;
                     mm = a > mm ? a : mm;
+                    mdiff |= b[u] != m0b;
                 }
             }
         }
@@ -119,6 +122,7 @@ k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t 
     s_m[tid] = mm;
     __syncthreads();
     if (nan) atomicOr(&s_nan, 1u << axis);
+    if (mdiff) atomicOr(&s_nan, 8u);   // bit 3: masses not all equal
     // thread d < dim reduces its axis (the threads with tid = d (mod dim):
     // the block's first index is a multiple of 6); thread 3 the masses
     if (tid < dim) {
@@ -168,7 +172,7 @@ k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t 
         }
         if ((tid & 31) == 0) s_red[k][tid >> 5] = a[k];
     }
-    if (nanmask) atomicOr(&s_nan, nanmask << 4);   // bits 4..6: the grid's NaN axes
+    if (nanmask) atomicOr(&s_nan, nanmask << 4);   // bits 4..6: the grid's NaN axes, 7: masses differ
     __syncthreads();
     if (tid < 7) {
         uint64_t acc = s_red[tid][0];
@@ -202,6 +206,14 @@ k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t 
         }
         box[11] = degenerate ? 1.0 : 0.0;
         for (int d = 0; d < 3; d++) box[12 + d] = (s_nan >> (4 + d)) & 1u ? 1.0 : 0.0;
+        // box[15]: every particle has the same positive, finite mass (the
+        // float-float traversal then measures masses in units of it)
+        bool unit = false;
+        if (mass && !((s_nan >> 7) & 1u)) {
+            const double m0 = mass[0];
+            unit = m0 > 0.0 && finite_bits((uint64_t)__double_as_longlong(m0));
+        }
+        box[15] = unit ? 1.0 : 0.0;
         *done_counter = 0;
     }
 }

@@ -5,6 +5,13 @@
 #pragma once
 #include "tree.cuh"
 
+// Accumulation two-sum of pair_ff_soft: 0 = FastTwoSum on the operands
+// ordered by magnitude (ALU compare and selects), 1 = Knuth's TwoSum (six
+// FP32 operations).  Both are exact; build-time switch for measurements.
+#ifndef BHUT_FF_KNUTH_ACC
+#define BHUT_FF_KNUTH_ACC 0
+#endif
+
 namespace bhut {
 
 // r^2 + eps^2 below this (normalised units) -> FP64 pair.  The coordinates
@@ -36,6 +43,19 @@ static __device__ void frame_from_box(const double* box, int dim, FastFrame* f)
     if (mm > 0.0) frexp(mm, &em);       // |m| <= 2^em
     f->ms = ldexp(1.0, -em);
     f->conv = ldexp(1.0, em - 2 * ex - 2);  // normalised -> physical acceleration (s^2 / ms)
+    f->unit = 0;
+}
+
+// Every particle has the same positive mass m0 (flag set by the
+// bounding-box kernel): masses are measured in units of m0, so a particle's
+// normalised mass is exactly 1 and a node's is M / m0 (FP64, then split hi +
+// lo).
+static __device__ void frame_unit_mass(double m0, bool uniform, FastFrame* f)
+{
+    if (!uniform || !(m0 > 0x1p-1000 && m0 < 0x1p+1000)) return;
+    f->ms = __drcp_rn(m0);
+    f->conv = __dmul_rn(__dmul_rn(m0, f->s), f->s);   // s a power of two: exact
+    f->unit = 1;
 }
 
 
@@ -160,6 +180,82 @@ __device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4
         al[k] = __fadd_rn(al[k], __fadd_rn(err, Fl));
     }
     return ok;
+}
+
+// The float-float pair term for a target inside the box when the softening
+// bounds R = |g|^2 + eps^2 from below ((eps s)^2 >= 2 kTinyR: no pair can go
+// to FP64).  Same inputs and result as pair_ff<DIM, false, false> up to the
+// last bits, with fewer operations:
+//  * the squares and eps^2 are non-negative, so each of the three additions
+//    of R's high part is Dekker's FastTwoSum on (max, min) (two min/max on
+//    the ALU pipe and three FP32 operations instead of Knuth's six);
+//  * R stays unnormalised as s + lo (|lo| <= 2^-22 s): the rsqrt is taken of
+//    s and the correction term e = 1 - (s + lo) y^2 absorbs lo;
+//  * w = y^3 (1 + 3e/2): |e| <= 2^-20.4 (MUFU error plus |lo| / s), so the
+//    dropped 15e^2/8 term is below 2^-39.9 of the pair, and in practice far
+//    below the 2^-48 representation of the coordinates (|g| is near-pair
+//    sized: ~2^-36 relative for a leaf pair);
+//  * the accumulation stays an exact two-sum, written as FastTwoSum on the
+//    operands ordered by magnitude (one compare and two selects on the ALU
+//    pipe, three FP32 operations);
+//  * UNIT: masses are in units of the common particle mass (every particle
+//    has mass exactly 1), so f = w and the mass product is skipped.
+template <int DIM, bool UNIT>
+__device__ __forceinline__ void pair_ff_soft(const float* Th, const float* Tl, float4 sh,
+                                             float4 sl, float e2h, float e2l, float* ah, float* al)
+{
+    float gh[3], gl[3], p[3], q[3];
+#pragma unroll
+    for (int k = 0; k < DIM; k++) {
+        const float d = __fsub_rn(comp(sh, k), Th[k]);   // exact on the grid
+        const float l = __fsub_rn(comp(sl, k), Tl[k]);   // exact on the lo grid
+        const float h = __fadd_rn(d, l);                  // FastTwoSum(d, l)
+        gl[k] = __fsub_rn(l, __fsub_rn(h, d));
+        gh[k] = h;
+        p[k] = __fmul_rn(h, h);
+        q[k] = __fmaf_rn(h, h, -p[k]);                   // exact square error
+    }
+    float c = __fmul_rn(gh[0], gl[0]);
+#pragma unroll
+    for (int k = 1; k < DIM; k++) c = __fmaf_rn(gh[k], gl[k], c);
+    // s = ((eps^2 + p0) + p1) + p2, each error exact
+    float s = e2h, lo = __fmaf_rn(2.0f, c, e2l);
+#pragma unroll
+    for (int k = 0; k < DIM; k++) {
+        const float a = fmaxf(s, p[k]), b = fminf(s, p[k]);
+        const float t = __fadd_rn(a, b);
+        lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(b, __fsub_rn(t, a)), q[k]));
+        s = t;
+    }
+    // y ~ s^(-1/2); A = (s + lo) y^2 - 1 = -e to ~2^-46
+    const float y = rsqrt_mufu(s);                    // s >= eps^2 > 0: normal
+    const float Y = __fmul_rn(y, y);
+    const float Ye = __fmaf_rn(y, y, -Y);
+    const float A = __fmaf_rn(s, Ye, __fmaf_rn(lo, Y, __fmaf_rn(s, Y, -1.0f)));
+    const float W = __fmul_rn(Y, y);
+    const float We = __fmaf_rn(Ye, y, __fmaf_rn(Y, y, -W));
+    const float wl = __fmaf_rn(__fmul_rn(W, -1.5f), A, We);   // y^3 (1 + 1.5 e) - W
+    float fh = W, fl = wl;
+    if (!UNIT) {
+        const float mh = sh.w, ml = sl.w;
+        fh = __fmul_rn(mh, W);
+        fl = __fmaf_rn(mh, wl, __fmaf_rn(ml, W, __fmaf_rn(mh, W, -fh)));
+    }
+#pragma unroll
+    for (int k = 0; k < DIM; k++) {
+        const float Fh = __fmul_rn(fh, gh[k]);
+        const float Fl = __fmaf_rn(fh, gl[k], __fmaf_rn(fl, gh[k], __fmaf_rn(fh, gh[k], -Fh)));
+        const float t = __fadd_rn(ah[k], Fh);
+#if BHUT_FF_KNUTH_ACC
+        const float err = two_sum_err(ah[k], Fh, t);
+#else
+        const bool sw = fabsf(Fh) > fabsf(ah[k]);
+        const float big = sw ? Fh : ah[k], small = sw ? ah[k] : Fh;
+        const float err = __fsub_rn(small, __fsub_rn(t, big));
+#endif
+        ah[k] = t;
+        al[k] = __fadd_rn(al[k], __fadd_rn(err, Fl));
+    }
 }
 
 // FP64 pair in physical units, G-less (the Numba loop arithmetic).

@@ -57,7 +57,10 @@ constexpr int kF32Unroll = BHUT_F32_UNROLL;
 // ---------------------------------------------------------------------------
 __global__ void k_frame(const double* __restrict__ box, int dim, FastFrame* __restrict__ f)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) frame_from_box(box, dim, f);
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        frame_from_box(box, dim, f);
+        frame_unit_mass(box[6], box[15] != 0.0, f);
+    }
 }
 
 __global__ void k_ff_particles(const double* __restrict__ sx, const double* __restrict__ sy,
@@ -73,7 +76,8 @@ __global__ void k_ff_particles(const double* __restrict__ sx, const double* __re
         split_grid(__dmul_rn(__dsub_rn(sy[i], f.c[1]), f.s), h.y, l.y);
         if (dim == 3) split_grid(__dmul_rn(__dsub_rn(sz[i], f.c[2]), f.s), h.z, l.z);
         else h.z = l.z = 0.0f;
-        split_plain(__dmul_rn(sm[i], f.ms), h.w, l.w);
+        if (f.unit) { h.w = 1.0f; l.w = 0.0f; }   // every mass is m0: exactly 1 in units of m0
+        else split_plain(__dmul_rn(sm[i], f.ms), h.w, l.w);
         ph[i] = h;
         pl[i] = l;
     }
@@ -171,7 +175,9 @@ struct FastArgs {
     int mac;                 // 0: reference criterion, 1: offset criterion (fp32 form)
 };
 
-template <int DIM, bool FAR, bool CHECK>
+// SOFT_PATH (= !FAR && !CHECK): every pair is taken by pair_ff_soft (no
+// FP64 fallback); UNIT: leaf pairs skip the mass product (unit masses).
+template <int DIM, bool FAR, bool CHECK, bool UNIT = false>
 __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const FastArgs& a,
                                      int w, int lane, bool valid, int64_t me_sorted, const float* Th,
                                      const float* Tl, float band_abs, double x, double y, double z,
@@ -213,10 +219,17 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                     // (bh.py:254).
                     cnt[0] += cn - (me_sorted >= s + b && me_sorted < s + b + cn);
                     unsigned fb = 0;   // pairs left to FP64 (rare), taken after the loop
+                    if (!FAR && !CHECK) {
 #pragma unroll (kFFUnroll)
-                    for (int q = 0; q < cn; q++)
-                        fb |= (unsigned)!pair_ff<DIM, FAR, CHECK>(Th, Tl, sh[w][q], sl[w][q],
-                                                                  a.e2h, a.e2l, ah, al) << q;
+                        for (int q = 0; q < cn; q++)
+                            pair_ff_soft<DIM, UNIT>(Th, Tl, sh[w][q], sl[w][q], a.e2h, a.e2l, ah,
+                                                    al);
+                    } else {
+#pragma unroll (kFFUnroll)
+                        for (int q = 0; q < cn; q++)
+                            fb |= (unsigned)!pair_ff<DIM, FAR, CHECK>(Th, Tl, sh[w][q], sl[w][q],
+                                                                      a.e2h, a.e2l, ah, al) << q;
+                    }
                     while (fb) {
                         const int gi = s + b + __ffs(fb) - 1;
                         fb &= fb - 1;
@@ -264,7 +277,9 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
             const unsigned omask = __ballot_sync(FULL, act && open);
             if (act && !open) {
                 const float4 nl = ft.nl[node];   // (cached: read by the opening test)
-                if (!pair_ff<DIM, FAR, CHECK>(Th, Tl, nh, nl, a.e2h, a.e2l, ah, al)) {
+                if (!FAR && !CHECK) {
+                    pair_ff_soft<DIM, false>(Th, Tl, nh, nl, a.e2h, a.e2l, ah, al);
+                } else if (!pair_ff<DIM, FAR, CHECK>(Th, Tl, nh, nl, a.e2h, a.e2l, ah, al)) {
                     const NodeCM cm = t.cm[node];
                     pair_fp64<DIM>(x, y, z, cm.x, cm.y, cm.z, cm.w, eps2, a64);
                     cnt[4]++;
@@ -327,6 +342,9 @@ k_traverse_fast(TreeDev t, FastTree ft, FastArgs a)
         if (__any_sync(FULL, far))
             walk<DIM, true, true>(t, ft, a, w, lane, valid, me_sorted, Th, Tl, band_abs, x, y, z,
                                   ah, al, a64, stack, sh, sl, cnt, overflow);
+        else if (SOFT && fr.unit)
+            walk<DIM, false, false, true>(t, ft, a, w, lane, valid, me_sorted, Th, Tl, band_abs, x,
+                                          y, z, ah, al, a64, stack, sh, sl, cnt, overflow);
         else
             walk<DIM, false, !SOFT>(t, ft, a, w, lane, valid, me_sorted, Th, Tl, band_abs, x, y, z,
                                     ah, al, a64, stack, sh, sl, cnt, overflow);

@@ -50,13 +50,16 @@ struct TopoTables {
 int make_topo_tables(int64_t n, int leaf_size, TopoTables* t);
 
 // Normalisation of the "fast" traversal: u = (x - c) * s with s a power of
-// two mapping the box into [-1, 1]; masses scaled by ms (a power of two);
-// physical acceleration = normalised acceleration * conv (= s^2 / ms).
+// two mapping the box into [-1, 1]; masses scaled by ms (a power of two, or
+// 1 / m0 when every particle has the same mass m0: unit = 1, particle masses
+// exactly 1); physical acceleration = normalised acceleration * conv
+// (= s^2 / ms, or s^2 m0).
 struct FastFrame {
     double c[3];
     double s;
     double ms;
     double conv;
+    int unit;
 };
 
 // Float-float copies of the particles (Morton order) and nodes.

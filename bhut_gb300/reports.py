@@ -4,6 +4,7 @@
     python -m bhut_gb300.reports batched [--nsys 2048]
     python -m bhut_gb300.reports served [--count 24] [--theta 0.7]
     python -m bhut_gb300.reports scaling [--sizes 1e5,1e6,4e6,16e6,64e6]
+    python -m bhut_gb300.reports build [--n 1000000] [--reps 10]
 
 ``precision``: the galaxy model (70 % exponential disc, 30 % Hernquist bulge,
 equal masses), softening 0.005, theta in {0.3, 0.5, 0.7}.  For each theta the
@@ -315,6 +316,48 @@ def scaling_report(sizes=(100_000, 1_000_000, 4_000_000, 16_000_000, 64_000_000)
     return lines
 
 
+def build_report(n: int = 1_000_000, reps: int = 10, leaf: int = 32, seed: int = 1):
+    """``build``: rebuilds of a Plummer sphere of n particles through one
+    persistent tree handle (staging copy + bounding box, Morton keys, radix
+    sort, gather, bottom-up moments: bhut.Tree.rebuild), then as many refits
+    in place (bottom-up moments only), the inputs resident on the device.
+    Each call is timed with CUDA events on the handle's stream; one JSON line
+    with the medians and the minima."""
+    import torch
+    from .api import _Handle
+    pos, m = workloads.plummer(int(n), seed=seed)
+    pd, md = torch.as_tensor(pos).cuda(), torch.as_tensor(m).cuda()
+    stream = torch.cuda.Stream()
+    h = _Handle(3, leaf, stream=stream.cuda_stream)
+    h.build(pd, md)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.rebuild(pd, md)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    refits = []   # refit in place (same topology: bhut.Tree.refit), positions moved
+    moved = pd + 1e-3 * torch.randn_like(pd)
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.refit_only(moved, md)
+        e1.record(stream)
+        e1.synchronize()
+        refits.append(e0.elapsed_time(e1))
+    h.close()
+    times.sort()
+    refits.sort()
+    line = {"report": "build", "n": int(n), "leaf_size": leaf, "reps": reps,
+            "rebuild_ms_median": times[len(times) // 2], "rebuild_ms_min": times[0],
+            "refit_ms_median": refits[len(refits) // 2], "refit_ms_min": refits[0]}
+    print(json.dumps(line), flush=True)
+    return line
+
+
 # ---------------------------------------------------------------------------
 # Sub-records of the benchmark line (bench.py): each bounded in time
 # ---------------------------------------------------------------------------
@@ -381,6 +424,66 @@ def exact_record(pos_d, m_d, *, theta: float, eps: float, G: float, leaf: int,
                                       "kernel)",
                          "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"},
             "interactions_per_solve": {"p2p": p2p, "m2p": m2p, "node_visits": visits}}
+
+
+def c1_record(*, n: int = 10_000, theta: float = 0.5, eps: float = 0.01, G: float = 1.0,
+              leaf: int = 32, steps: int = 50, e2e_calls: int = 20,
+              fma_rate: float | None = None):
+    """The reference's CPU-runnable workload: n Gaussian particles (seed 0,
+    unit masses), theta 0.5, softening 0.01, leaf 32, self accelerations,
+    form "fast".  Device time of rebuild + traversal through one persistent
+    handle (CUDA events, median of ``steps``), and end to end through
+    bhut_gb300.accelerations with host NumPy buffers.  Returns the record
+    and the accelerations (for the caller's CPU comparison)."""
+    import torch
+    from .api import _Handle
+    pos, m = workloads.gaussian(n, seed=0)
+    pd, md = torch.as_tensor(pos).cuda(), torch.as_tensor(m).cuda()
+    out = torch.empty_like(pd)
+    stream = torch.cuda.Stream()
+    h = _Handle(3, leaf, stream=stream.cuda_stream)
+    h.set_form("fast")
+    h.build(pd, md)
+    h.accel_self(theta, eps, G, out)
+    torch.cuda.synchronize()
+    tot, trav = [], []
+    for _ in range(steps):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        h.rebuild(pd, md)
+        e1.record(stream)
+        h.accel_self(theta, eps, G, out)
+        e2.record(stream)
+        e2.synchronize()
+        tot.append(e0.elapsed_time(e2) / 1e3)
+        trav.append(e1.elapsed_time(e2) / 1e3)
+    p2p, m2p, visits = h.stats()
+    h.close()
+    tot.sort()
+    trav.sort()
+    t_step, t_trav = tot[len(tot) // 2], trav[len(trav) // 2]
+    api.accelerations(pos, m, theta=theta, softening=eps, G=G, leaf_size=leaf)
+    t0 = time.perf_counter()
+    for _ in range(e2e_calls):
+        acc = api.accelerations(pos, m, theta=theta, softening=eps, G=G, leaf_size=leaf)
+    t_e2e = (time.perf_counter() - t0) / e2e_calls
+    rec = {"workload": f"Gaussian N={n:,} (standard normal positions, seed 0, unit masses), "
+                       f"theta={theta}, softening={eps}, G={G}, leaf_size={leaf}, self "
+                       "accelerations, form fast",
+           "accels_per_s": n / t_step, "solve_ms_median": t_step * 1e3,
+           "traversal_ms_median": t_trav * 1e3, "steps": steps,
+           "e2e": {"value": n / t_e2e, "unit": "accels/s", "api": "bhut_gb300.accelerations",
+                   "timed_calls": e2e_calls, "h2d_bytes_per_call": int(pos.nbytes + m.nbytes),
+                   "d2h_bytes_per_call": int(acc.nbytes)},
+           "interactions_per_solve": {"p2p": p2p, "m2p": m2p, "node_visits": visits}}
+    if fma_rate:
+        instr = 93 * p2p + 97 * m2p
+        rec["roofline"] = {"bound": "fp32", "kernel": "k_traverse_fast",
+                           "achieved": instr / t_trav / 1e12, "peak": fma_rate,
+                           "unit": "T instr/s", "frac": instr / t_trav / 1e12 / fma_rate,
+                           "note": "313 warps of targets for 152 SMs: latency-bound at this "
+                                   "size (the traversal time includes the launch)"}
+    return rec, np.asarray(acc), (pos, m)
 
 
 def batched_record(*, nsys: int = 2048, nmin: int = 256, nmax: int = 65536, seed: int = 11,
@@ -596,11 +699,13 @@ def served_record(*, count: int = 200, rate: float = 200.0, steps: int = 100, se
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("report", choices=["precision", "batched", "served", "scaling"])
+    ap.add_argument("report", choices=["precision", "batched", "served", "scaling", "build"])
+    ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--sizes", default="1e5,1e6,4e6,16e6,64e6")
     ap.add_argument("--count", type=int, default=24)
     ap.add_argument("--nsys", type=int, default=2048)
-    ap.add_argument("--n", type=int, default=4_000_000)
+    ap.add_argument("--n", type=int, default=None,
+                    help="particles (precision: 4,000,000; build: 1,000,000)")
     ap.add_argument("--sample", type=int, default=8192)
     ap.add_argument("--criterion", default=None)
     ap.add_argument("--multipole", default=None)
@@ -609,13 +714,15 @@ def main():
     ap.add_argument("--plain-theta-equal", type=float, default=None)
     args = ap.parse_args()
     if args.report == "precision":
-        precision_report(args.n, args.sample, criterion=args.criterion or "bh",
+        precision_report(args.n or 4_000_000, args.sample, criterion=args.criterion or "bh",
                          multipole=args.multipole or "mono",
                          thetas=tuple(float(x) for x in args.thetas.split(",")))
     elif args.report == "batched":
         batched_report(args.nsys, criterion=args.criterion or "bh",
                        multipole=args.multipole or "mono",
                        theta=args.theta if args.theta is not None else 0.5)
+    elif args.report == "build":
+        build_report(args.n or 1_000_000, args.reps)
     elif args.report == "scaling":
         scaling_report(tuple(int(float(x)) for x in args.sizes.split(",")))
     elif args.report == "served":
