@@ -478,8 +478,7 @@ def run_ours(args, ws, rank, local):
             line["precision"] = reports.precision_record(fma_rate=fma_rate)
         if not args.no_served:
             line["served"] = reports.served_record(
-                count=args.served_count, server_seconds=args.served_seconds,
-                plain_seconds=args.served_seconds, fast_seconds=args.served_fast_seconds)
+                count=args.served_count, server_seconds=args.served_seconds)
     if not args.no_cpu_baseline:
         cb = cpu_solve_sample(pos, m, args.cpu_sample)
         line["cpu_baseline"] = {
@@ -538,9 +537,7 @@ def main():
                     help="skip the served-stream comparison (about two minutes)")
     ap.add_argument("--served-count", type=int, default=200)
     ap.add_argument("--served-seconds", type=float, default=45.0,
-                    help="wall-time cap of the server and of the plain same-config leg")
-    ap.add_argument("--served-fast-seconds", type=float, default=20.0,
-                    help="wall-time cap of the plain FP64-accurate leg")
+                    help="window of the open-loop stream comparison")
     args = ap.parse_args()
     if args.form is None:
         from bhut_gb300.api import DEFAULT_FORM

@@ -1,8 +1,14 @@
 // Batched form: many independent N-body systems solved in one pass.
 //
-// The systems are concatenated (CSR offsets).  The build is segmented:
-//   k_seg_bbox        one block per system: box + max |m|
-//   k_seg_morton      one block per system: Morton keys in that system's box
+// The systems are concatenated (CSR offsets).  The build is segmented, and
+// every per-solve kernel spreads its work over the particles (or nodes), not
+// over the systems, so that one large system is not left to one block:
+//   k_seg_acc_init    per-system accumulators cleared
+//   k_seg_bbox_chunks one block per chunk of <= kSegChunk particles of one
+//                     system: box, max |m|, equal-mass test, merged into the
+//                     system's accumulators with 64-bit integer atomics
+//   k_seg_box_finish  per system: box, Morton quantiser data, frame
+//   k_seg_morton      per particle: Morton key in its system's box
 //   radix_sort_pairs  by Morton key, then (stable) by system id
 //   k_gather_sorted   sorted SoA (global)
 //   k_seg_topology    one block per system: the count-split topology of
@@ -10,8 +16,9 @@
 //                     offset into one forest (cached while the layout holds)
 //   k_bottom_up       shared with the single-tree engine (leaves of all
 //                     systems climb their own tree)
-//   k_seg_frames      one block per system: normalisation frame, float-float
-//                     particles and nodes
+//   k_seg_ff_particles, k_seg_ff_nodes
+//                     per particle / node: float-float copies in the system's
+//                     frame
 // and the traversal is one persistent kernel: every warp pulls
 // (system, target chunk) tasks from a global atomic counter (heaviest systems
 // first) until the queue is empty -- no warp waits on another.  Each task is
@@ -40,104 +47,164 @@ constexpr int kBatchThreads = kBatchWarps * kWarp;
 // ---------------------------------------------------------------------------
 // segmented build kernels
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kSegThreads)
-k_seg_bbox(const double* __restrict__ pos, const double* __restrict__ mass,
-           const int64_t* __restrict__ off, int dim, double* __restrict__ box,
-           unsigned* __restrict__ err)
+// Per-system accumulators (kSegAcc x uint64 per system): ordered images of
+// min x, y, z and of max x, y, z, the bits of max |mass|, flags (bit 0: a
+// mass differs from the system's first, bit 1: a particle lies beyond 1.1x
+// the system's root box).
+constexpr int kSegAcc = 8;
+constexpr int kSegChunk = 4096;   // particles per block of the chunked box
+// Per-system box (kSegBox doubles): min (0..2), max (3..5), max |m| (6),
+// equal positive masses (7), RN(1 / extent) (8..10), zero extent on some
+// axis (11), extent (12..14; 1 for a zero extent).
+constexpr int kSegBox = 16;
+
+__global__ void k_seg_acc_init(uint64_t* __restrict__ acc, int64_t ns)
 {
-    const int s = blockIdx.x;
-    const int64_t p0 = off[s], p1 = off[s + 1];
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    double mm = 0.0;
-    bool bad = false, mdiff = false;
-    const double m0 = p1 > p0 ? mass[p0] : 0.0;
-    for (int64_t i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
-        for (int d = 0; d < dim; d++) {
-            const double v = pos[i * dim + d];
-            bad |= !isfinite(v);
-            lo[d] = v < lo[d] ? v : lo[d];
-            hi[d] = v > hi[d] ? v : hi[d];
-        }
-        const double am = fabs(mass[i]);
-        bad |= !isfinite(am);
-        mdiff |= __double_as_longlong(mass[i]) != __double_as_longlong(m0);
-        mm = am > mm ? am : mm;
-    }
-    __shared__ double red[kSegThreads / 32][7];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) {
-        for (int d = 0; d < 3; d++) {
-            const double a = __shfl_down_sync(0xffffffffu, lo[d], o);
-            const double b = __shfl_down_sync(0xffffffffu, hi[d], o);
-            lo[d] = a < lo[d] ? a : lo[d];
-            hi[d] = b > hi[d] ? b : hi[d];
-        }
-        const double c = __shfl_down_sync(0xffffffffu, mm, o);
-        mm = c > mm ? c : mm;
-    }
-    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(err, kErrNonFinite);
-    if (lane == 0) {
-        for (int d = 0; d < 3; d++) { red[warp][d] = lo[d]; red[warp][3 + d] = hi[d]; }
-        red[warp][6] = mm;
-    }
-    // every mass of the system bit-equal to the first (unit-mass frame)
-    const bool uniform = !__syncthreads_or(mdiff);
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < kSegThreads / 32; w++) {
-            for (int d = 0; d < 3; d++) {
-                lo[d] = red[w][d] < lo[d] ? red[w][d] : lo[d];
-                hi[d] = red[w][3 + d] > hi[d] ? red[w][3 + d] : hi[d];
-            }
-            mm = red[w][6] > mm ? red[w][6] : mm;
-        }
-        for (int d = 0; d < 3; d++) { box[s * 8 + d] = lo[d]; box[s * 8 + 3 + d] = hi[d]; }
-        box[s * 8 + 6] = mm;
-        box[s * 8 + 7] = uniform && m0 > 0.0 && isfinite(m0) ? 1.0 : 0.0;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ns;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t* a = acc + kSegAcc * s;
+        a[0] = a[1] = a[2] = ~0ull;
+        a[3] = a[4] = a[5] = a[6] = a[7] = 0ull;
     }
 }
 
+// One block per chunk: chunk c covers particles [chunks[c].y, min(chunks[c].y
+// + kSegChunk, part_off[s + 1])) of system s = chunks[c].x.  The chunk's
+// coordinates are read as one flat run of doubles (coalesced).
+template <int DIM>
 __global__ void __launch_bounds__(kSegThreads)
-k_seg_morton(const double* __restrict__ pos, const int64_t* __restrict__ off, int dim,
-             const double* __restrict__ box, uint64_t* __restrict__ keys,
-             int32_t* __restrict__ idx, int32_t* __restrict__ sys_of)
+k_seg_bbox_chunks(const double* __restrict__ pos, const double* __restrict__ mass,
+                  const int64_t* __restrict__ part_off, const int2* __restrict__ chunks,
+                  uint64_t* __restrict__ acc, unsigned* __restrict__ err)
+{
+    const int2 ch = chunks[blockIdx.x];
+    const int s = ch.x;
+    const int64_t p0 = ch.y, p1 = min(p0 + (int64_t)kSegChunk, part_off[s + 1]);
+    const uint64_t* __restrict__ pb = reinterpret_cast<const uint64_t*>(pos);
+    const uint64_t* __restrict__ mb = reinterpret_cast<const uint64_t*>(mass);
+    uint64_t v[7] = {~0ull, ~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull};
+    bool bad = false, mdiff = false;
+    for (int64_t j = p0 * DIM + threadIdx.x; j < p1 * DIM; j += blockDim.x) {
+        const uint64_t x = __ldg(pb + j);
+        const int d = (int)(j % DIM);
+        bad |= !finite_bits(x);
+        const uint64_t k = ord_key(x);
+        v[d] = k < v[d] ? k : v[d];
+        v[3 + d] = k > v[3 + d] ? k : v[3 + d];
+    }
+    const uint64_t m0 = __ldg(mb + part_off[s]);
+    for (int64_t i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
+        const uint64_t x = __ldg(mb + i);
+        bad |= !finite_bits(x);
+        const uint64_t am = x & 0x7FFFFFFFFFFFFFFFull;
+        v[6] = am > v[6] ? am : v[6];
+        mdiff |= x != m0;
+    }
+    __shared__ uint64_t red[kSegThreads / 32][7];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint64_t y = __shfl_down_sync(0xffffffffu, v[k], o);
+            v[k] = k < 3 ? (y < v[k] ? y : v[k]) : (y > v[k] ? y : v[k]);
+        }
+        if (lane == 0) red[warp][k] = v[k];
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(err, kErrNonFinite);
+    mdiff = __syncthreads_or(mdiff);
+    if (threadIdx.x < 7) {
+        const int k = threadIdx.x;
+        uint64_t r = red[0][k];
+        for (int w = 1; w < kSegThreads / 32; w++)
+            r = k < 3 ? (red[w][k] < r ? red[w][k] : r) : (red[w][k] > r ? red[w][k] : r);
+        unsigned long long* a = reinterpret_cast<unsigned long long*>(acc + kSegAcc * s + k);
+        if (k < 3) {
+            if (k < DIM) atomicMin(a, (unsigned long long)r);
+        } else if (k < 6) {
+            if (k - 3 < DIM) atomicMax(a, (unsigned long long)r);
+        } else {
+            atomicMax(a, (unsigned long long)r);
+        }
+    }
+    if (threadIdx.x == 0 && mdiff)
+        atomicOr(reinterpret_cast<unsigned long long*>(acc + kSegAcc * s + 7), 1ull);
+}
+
+// Per system: the box from the accumulators, the Morton quantiser's data
+// (the same arithmetic as the single-tree k_bbox / k_morton) and the
+// float-float frame.
+__global__ void k_seg_box_finish(const uint64_t* __restrict__ acc, const double* __restrict__ mass,
+                                 const int64_t* __restrict__ part_off, int dim, int64_t ns,
+                                 double* __restrict__ box, FastFrame* __restrict__ frames)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ns;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t* a = acc + kSegAcc * s;
+        double* bx = box + kSegBox * s;
+        bool degenerate = false;
+        for (int d = 0; d < 3; d++) {
+            double lo = 0.0, hi = 0.0, ext = 1.0, rcp = 1.0;
+            if (d < dim) {
+                lo = __longlong_as_double((long long)ord_inv(a[d]));
+                hi = __longlong_as_double((long long)ord_inv(a[3 + d]));
+                const double e = __dsub_rn(hi, lo);
+                ext = e <= 0 ? 1.0 : e;
+                degenerate |= e <= 0;
+                rcp = __drcp_rn(ext);
+            }
+            bx[d] = lo;
+            bx[3 + d] = hi;
+            bx[8 + d] = rcp;
+            bx[12 + d] = ext;
+        }
+        bx[6] = __longlong_as_double((long long)a[6]);
+        const double m0 = mass[part_off[s]];
+        const bool unit = !(a[7] & 1ull) && m0 > 0.0 && isfinite(m0);
+        bx[7] = unit ? 1.0 : 0.0;
+        bx[11] = degenerate ? 1.0 : 0.0;
+        FastFrame f;
+        frame_from_box(bx, dim, &f);
+        frame_unit_mass(bx[6], unit, &f);
+        frames[s] = f;
+    }
+}
+
+// Morton keys, each particle in its own system's box (sys_of: the system of
+// every particle; input and sorted order share the systems' ranges).
+template <int DIM>
+__global__ void k_seg_morton(const double* __restrict__ pos, int64_t n,
+                             const int32_t* __restrict__ sys_of, const double* __restrict__ box,
+                             uint64_t* __restrict__ keys, int32_t* __restrict__ idx)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double* bx = box + kSegBox * sys_of[i];
+        uint64_t c[3] = {0, 0, 0};
+        if (bx[11] == 0.0) {   // division-free quantiser
+#pragma unroll
+            for (int d = 0; d < DIM; d++)
+                c[d] = quantise_rcp(pos[DIM * i + d], bx[d], bx[12 + d], bx[8 + d]);
+        } else {
+#pragma unroll
+            for (int d = 0; d < DIM; d++)
+                c[d] = quantise(pos[DIM * i + d], bx[d], bx[12 + d],
+                                __dsub_rn(bx[3 + d], bx[d]) <= 0 ? 0.5 : 0.0);
+        }
+        keys[i] = DIM == 3 ? morton3(c[0], c[1], c[2]) : morton2(c[0], c[1]);
+        idx[i] = (int32_t)i;
+    }
+}
+
+// The system of every particle and of every node (once per layout).
+__global__ void __launch_bounds__(kSegThreads)
+k_seg_owner(const int64_t* __restrict__ part_off, const int64_t* __restrict__ node_off,
+            int32_t* __restrict__ sys_of, int32_t* __restrict__ node_sys)
 {
     const int s = blockIdx.x;
-    const int64_t p0 = off[s], p1 = off[s + 1];
-    const double* bx = box + s * 8;
-    double pmin[3], ext[3], offs[3], rcp[3];
-    bool degenerate = false;
-    for (int d = 0; d < 3; d++) { pmin[d] = 0.0; ext[d] = 1.0; offs[d] = 0.0; rcp[d] = 1.0; }
-    for (int d = 0; d < dim; d++) {
-        pmin[d] = bx[d];
-        const double e = __dsub_rn(bx[3 + d], bx[d]);
-        ext[d] = e <= 0 ? 1.0 : e;
-        offs[d] = e <= 0 ? 0.5 : 0.0;
-        degenerate |= e <= 0;
-        rcp[d] = __drcp_rn(ext[d]);
-    }
-    for (int64_t i = p0 + threadIdx.x; i < p1; i += blockDim.x) {
-        uint64_t key;
-        if (!degenerate) {   // division-free quantiser (uniform branch per system)
-            if (dim == 3) {
-                key = morton3(quantise_rcp(pos[3 * i], pmin[0], ext[0], rcp[0]),
-                              quantise_rcp(pos[3 * i + 1], pmin[1], ext[1], rcp[1]),
-                              quantise_rcp(pos[3 * i + 2], pmin[2], ext[2], rcp[2]));
-            } else {
-                key = morton2(quantise_rcp(pos[2 * i], pmin[0], ext[0], rcp[0]),
-                              quantise_rcp(pos[2 * i + 1], pmin[1], ext[1], rcp[1]));
-            }
-        } else if (dim == 3) {
-            key = morton3(quantise(pos[3 * i], pmin[0], ext[0], offs[0]),
-                          quantise(pos[3 * i + 1], pmin[1], ext[1], offs[1]),
-                          quantise(pos[3 * i + 2], pmin[2], ext[2], offs[2]));
-        } else {
-            key = morton2(quantise(pos[2 * i], pmin[0], ext[0], offs[0]),
-                          quantise(pos[2 * i + 1], pmin[1], ext[1], offs[1]));
-        }
-        keys[i] = key;
-        idx[i] = (int32_t)i;
+    for (int64_t i = part_off[s] + threadIdx.x; i < part_off[s + 1]; i += blockDim.x)
         sys_of[i] = s;
-    }
+    for (int64_t k = node_off[s] + threadIdx.x; k < node_off[s + 1]; k += blockDim.x)
+        node_sys[k] = s;
 }
 
 __global__ void k_seg_key2(const int32_t* __restrict__ perm, const int32_t* __restrict__ sys_of,
@@ -151,12 +218,13 @@ __global__ void k_seg_key2(const int32_t* __restrict__ perm, const int32_t* __re
 // Systems marked in `keep` reuse the permutation given by the caller (a
 // refit: their Morton order and topology are frozen, node boxes and moments
 // are recomputed from the new positions); the others keep the fresh sort.
-__global__ void k_seg_keep_perm(const int64_t* __restrict__ off, const uint8_t* __restrict__ keep,
+__global__ void k_seg_keep_perm(int64_t n, const int32_t* __restrict__ sys_of,
+                                const uint8_t* __restrict__ keep,
                                 const int32_t* __restrict__ perm_in, int32_t* __restrict__ perm)
 {
-    const int s = blockIdx.x;
-    if (!keep[s]) return;
-    for (int64_t i = off[s] + threadIdx.x; i < off[s + 1]; i += blockDim.x) perm[i] = perm_in[i];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        if (keep[sys_of[i]]) perm[i] = perm_in[i];
 }
 
 // should_refit_vs_rebuild (bhut/tree/refit.py:236-249) per system: flag[s]
@@ -185,28 +253,41 @@ __global__ void k_seg_outside(const double* __restrict__ pos, const int64_t* __r
 
 // The same test on the device inside a solve: a system asked to keep its
 // order (keep[s] = 1) that has a particle beyond 1.1 x its stored root box is
-// rebuilt instead (keep[s] <- 0, forced[s] += 1).
-__global__ void k_seg_keep_outside(const double* __restrict__ pos, const int64_t* __restrict__ off,
-                                   const double* __restrict__ roots, int dim,
-                                   uint8_t* __restrict__ keep, int32_t* __restrict__ forced)
+// rebuilt instead (keep[s] <- 0, forced[s] += 1).  Per particle, the finding
+// goes to flag bit 1 of the system's accumulators; k_seg_keep_finish applies
+// it per system.
+__global__ void k_seg_keep_outside(const double* __restrict__ pos, int64_t n, int dim,
+                                   const int32_t* __restrict__ sys_of,
+                                   const double* __restrict__ roots,
+                                   const uint8_t* __restrict__ keep, uint64_t* __restrict__ acc)
 {
-    const int s = blockIdx.x;
-    if (!keep[s]) return;
-    const double* r = roots + 4 * s;
-    const double lim = __dmul_rn(1.1, r[3]);
-    bool out = false;
-    for (int64_t i = off[s] + threadIdx.x; i < off[s + 1]; i += blockDim.x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int s = sys_of[i];
+        if (!keep[s]) continue;
+        const double* r = roots + 4 * s;
+        const double lim = __dmul_rn(1.1, r[3]);
         double mx = fabs(__dsub_rn(pos[i * dim], r[0]));
         for (int d = 1; d < dim; d++) {
             const double v = fabs(__dsub_rn(pos[i * dim + d], r[d]));
             mx = v > mx ? v : mx;
         }
-        out |= (mx > lim) || !(mx == mx);
+        if ((mx > lim) || !(mx == mx)) {
+            unsigned long long* f = reinterpret_cast<unsigned long long*>(acc + kSegAcc * s + 7);
+            if (!(*f & 2ull)) atomicOr(f, 2ull);
+        }
     }
-    out = __syncthreads_or(out);
-    if (threadIdx.x == 0 && out) {
-        keep[s] = 0;
-        forced[s] += 1;
+}
+
+__global__ void k_seg_keep_finish(const uint64_t* __restrict__ acc, int64_t ns,
+                                  uint8_t* __restrict__ keep, int32_t* __restrict__ forced)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ns;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        if (keep[s] && (acc[kSegAcc * s + 7] & 2ull)) {
+            keep[s] = 0;
+            forced[s] += 1;
+        }
     }
 }
 
@@ -325,25 +406,15 @@ k_seg_topology(const int64_t* __restrict__ part_off, const int64_t* __restrict__
     }
 }
 
-// One block per system: frame, float-float particles and nodes.
-__global__ void __launch_bounds__(kSegThreads)
-k_seg_frames(TreeDev t, const int64_t* __restrict__ part_off, const int64_t* __restrict__ node_off,
-             const double* __restrict__ box, const double* __restrict__ center,
-             FastFrame* __restrict__ frames, float4* __restrict__ ph, float4* __restrict__ pl,
-             float4* __restrict__ nh, float4* __restrict__ nl, float* __restrict__ nsize,
-             float* __restrict__ ndelta, const double* __restrict__ quad, float4* __restrict__ nq0,
-             float2* __restrict__ nq1, int4* __restrict__ nhdr)
+// Float-float copies of every particle and node in its system's frame.
+__global__ void k_seg_ff_particles(TreeDev t, const int32_t* __restrict__ sys_of,
+                                   const FastFrame* __restrict__ frames, float4* __restrict__ ph,
+                                   float4* __restrict__ pl)
 {
-    const int s = blockIdx.x;
     const int dim = t.dim;
-    __shared__ FastFrame f;
-    if (threadIdx.x == 0) {
-        frame_from_box(box + s * 8, dim, &f);
-        frame_unit_mass(box[s * 8 + 6], box[s * 8 + 7] != 0.0, &f);
-        frames[s] = f;
-    }
-    __syncthreads();
-    for (int64_t i = part_off[s] + threadIdx.x; i < part_off[s + 1]; i += blockDim.x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < t.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const FastFrame& f = frames[sys_of[i]];
         float4 h, l;
         split_grid(__dmul_rn(__dsub_rn(t.sx[i], f.c[0]), f.s), h.x, l.x);
         split_grid(__dmul_rn(__dsub_rn(t.sy[i], f.c[1]), f.s), h.y, l.y);
@@ -354,9 +425,21 @@ k_seg_frames(TreeDev t, const int64_t* __restrict__ part_off, const int64_t* __r
         ph[i] = h;
         pl[i] = l;
     }
-    for (int64_t k = node_off[s] + threadIdx.x; k < node_off[s + 1]; k += blockDim.x) {
-        const NodeCM c = t.cm[k];
+}
 
+__global__ void k_seg_ff_nodes(TreeDev t, const int32_t* __restrict__ node_sys,
+                               const FastFrame* __restrict__ frames,
+                               const double* __restrict__ center, float4* __restrict__ nh,
+                               float4* __restrict__ nl, float* __restrict__ nsize,
+                               float* __restrict__ ndelta, const double* __restrict__ quad,
+                               float4* __restrict__ nq0, float2* __restrict__ nq1,
+                               int4* __restrict__ nhdr)
+{
+    const int dim = t.dim;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < t.m;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const FastFrame& f = frames[node_sys[k]];
+        const NodeCM c = t.cm[k];
         float4 h, l;
         split_grid(__dmul_rn(__dsub_rn(c.x, f.c[0]), f.s), h.x, l.x);
         split_grid(__dmul_rn(__dsub_rn(c.y, f.c[1]), f.s), h.y, l.y);
@@ -788,7 +871,9 @@ struct bhut_batch {
     BufB pos, mass, d_part_off, d_node_off, d_leaf_off, d_tasks, keys, perm, sys_of, key2,
         sx, sy, sz, sm, cm, size, center, half, lo, hi, first_child, start, count, parent,
         leaf_list, arrive, sort_scratch, box, frames, ph, pl, nh, nl, nsize, ndelta, counter,
-        err, stats, out, keep, perm_in, quad, nq0, nq1, nhdr, roots, forced, frontier;
+        err, stats, out, keep, perm_in, quad, nq0, nq1, nhdr, roots, forced, frontier,
+        node_sys, acc, d_chunks;
+    int64_t nchunks = 0;
     bool keep_active = false;
     unsigned long long last_stats[5] = {0, 0, 0, 0, 0};
     cudaGraphExec_t graph = nullptr;
@@ -804,7 +889,7 @@ struct bhut_batch {
                         &first_child, &start, &count, &parent, &leaf_list, &arrive,
                         &sort_scratch, &box, &frames, &ph, &pl, &nh, &nl, &nsize, &ndelta,
                         &counter, &err, &stats, &out, &keep, &perm_in, &quad, &nq0, &nq1, &nhdr,
-                        &roots, &forced, &frontier})
+                        &roots, &forced, &frontier, &node_sys, &acc, &d_chunks})
             x->release(stream);
     }
 
@@ -914,7 +999,26 @@ int plan_layout(bhut_batch* b, const int64_t* offsets, int64_t nsys)
     BHUT_TRY(b->nq0.ensure(sizeof(float4) * mtot, s));
     BHUT_TRY(b->nq1.ensure(sizeof(float2) * mtot, s));
     BHUT_TRY(b->nhdr.ensure(sizeof(int4) * mtot, s));
-    BHUT_TRY(b->box.ensure(sizeof(double) * 8 * nsys, s));
+    BHUT_TRY(b->box.ensure(sizeof(double) * kSegBox * nsys, s));
+    BHUT_TRY(b->acc.ensure(sizeof(uint64_t) * kSegAcc * nsys, s));
+    BHUT_TRY(b->node_sys.ensure(sizeof(int32_t) * mtot, s));
+    {   // chunks of at most kSegChunk particles, each inside one system
+        std::vector<int2> ch;
+        for (int64_t q = 0; q < nsys; q++)
+            for (int64_t p = b->part_off[q]; p < b->part_off[q + 1]; p += kSegChunk)
+                ch.push_back(make_int2((int)q, (int)p));
+        b->nchunks = (int64_t)ch.size();
+        BHUT_TRY(b->d_chunks.ensure(sizeof(int2) * ch.size(), s));
+        BHUT_CUDA(cudaMemcpyAsync(b->d_chunks.p, ch.data(), sizeof(int2) * ch.size(),
+                                  cudaMemcpyHostToDevice, s));
+        BHUT_CUDA(cudaStreamSynchronize(s));   // the host vector goes out of scope
+    }
+    k_seg_owner<<<(unsigned)nsys, kSegThreads, 0, s>>>(b->d_part_off.as<int64_t>(),
+                                                       b->d_node_off.as<int64_t>(),
+                                                       b->sys_of.as<int32_t>(),
+                                                       b->node_sys.as<int32_t>());
+    BHUT_CUDA(cudaGetLastError());
+    note_launches(1);
     BHUT_TRY(b->frames.ensure(sizeof(FastFrame) * nsys, s));
     BHUT_TRY(b->sort_scratch.ensure(sort_scratch_bytes(b->ntot), s));
     BHUT_TRY(b->counter.ensure(sizeof(unsigned) * 4, s));
@@ -962,16 +1066,33 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
     cudaStream_t s = b->stream;
     const int dim = b->dim;
     const int64_t ns = b->nsys, n = b->ntot;
-    k_seg_bbox<<<(unsigned)ns, kSegThreads, 0, s>>>(b->pos.as<double>(), b->mass.as<double>(),
-                                                    b->d_part_off.as<int64_t>(), dim,
-                                                    b->box.as<double>(), b->err.as<unsigned>());
-    k_seg_morton<<<(unsigned)ns, kSegThreads, 0, s>>>(b->pos.as<double>(),
-                                                      b->d_part_off.as<int64_t>(), dim,
-                                                      b->box.as<double>(), b->keys.as<uint64_t>(),
-                                                      b->perm.as<int32_t>(),
-                                                      b->sys_of.as<int32_t>());
+    const unsigned gs = grid_for(ns, 128);
+    k_seg_acc_init<<<gs, 128, 0, s>>>(b->acc.as<uint64_t>(), ns);
+    if (dim == 3)
+        k_seg_bbox_chunks<3><<<(unsigned)b->nchunks, kSegThreads, 0, s>>>(
+            b->pos.as<double>(), b->mass.as<double>(), b->d_part_off.as<int64_t>(),
+            b->d_chunks.as<int2>(), b->acc.as<uint64_t>(), b->err.as<unsigned>());
+    else
+        k_seg_bbox_chunks<2><<<(unsigned)b->nchunks, kSegThreads, 0, s>>>(
+            b->pos.as<double>(), b->mass.as<double>(), b->d_part_off.as<int64_t>(),
+            b->d_chunks.as<int2>(), b->acc.as<uint64_t>(), b->err.as<unsigned>());
+    k_seg_box_finish<<<gs, 128, 0, s>>>(b->acc.as<uint64_t>(), b->mass.as<double>(),
+                                        b->d_part_off.as<int64_t>(), dim, ns, b->box.as<double>(),
+                                        b->frames.as<FastFrame>());
+    if (dim == 3)
+        k_seg_morton<3><<<grid_for(n, 256), 256, 0, s>>>(b->pos.as<double>(), n,
+                                                         b->sys_of.as<int32_t>(),
+                                                         b->box.as<double>(),
+                                                         b->keys.as<uint64_t>(),
+                                                         b->perm.as<int32_t>());
+    else
+        k_seg_morton<2><<<grid_for(n, 256), 256, 0, s>>>(b->pos.as<double>(), n,
+                                                         b->sys_of.as<int32_t>(),
+                                                         b->box.as<double>(),
+                                                         b->keys.as<uint64_t>(),
+                                                         b->perm.as<int32_t>());
     BHUT_CUDA(cudaGetLastError());
-    note_launches(2);
+    note_launches(4);
     BHUT_TRY(radix_sort_pairs(b->keys.as<uint64_t>(), b->perm.as<int32_t>(), n,
                               dim == 3 ? 63 : 42, b->sort_scratch.p, s));
     if (ns > 1) {
@@ -984,16 +1105,18 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
     }
     if (b->keep_active) {
         if (b->refit_rule) {
-            k_seg_keep_outside<<<(unsigned)ns, kSegThreads, 0, s>>>(
-                b->pos.as<double>(), b->d_part_off.as<int64_t>(), b->roots.as<double>(), dim,
-                b->keep.as<uint8_t>(), b->forced.as<int32_t>());
+            k_seg_keep_outside<<<grid_for(n, 256), 256, 0, s>>>(
+                b->pos.as<double>(), n, dim, b->sys_of.as<int32_t>(), b->roots.as<double>(),
+                b->keep.as<uint8_t>(), b->acc.as<uint64_t>());
+            k_seg_keep_finish<<<gs, 128, 0, s>>>(b->acc.as<uint64_t>(), ns,
+                                                  b->keep.as<uint8_t>(), b->forced.as<int32_t>());
             BHUT_CUDA(cudaGetLastError());
-            note_launches(1);
+            note_launches(2);
         }
-        k_seg_keep_perm<<<(unsigned)ns, kSegThreads, 0, s>>>(b->d_part_off.as<int64_t>(),
-                                                           b->keep.as<uint8_t>(),
-                                                           b->perm_in.as<int32_t>(),
-                                                           b->perm.as<int32_t>());
+        k_seg_keep_perm<<<grid_for(n, 256), 256, 0, s>>>(n, b->sys_of.as<int32_t>(),
+                                                          b->keep.as<uint8_t>(),
+                                                          b->perm_in.as<int32_t>(),
+                                                          b->perm.as<int32_t>());
         BHUT_CUDA(cudaGetLastError());
         note_launches(1);
     }
@@ -1023,14 +1146,16 @@ int enqueue_solve(bhut_batch* b, double theta, double eps, double G, double* out
                                     b->arrive.as<unsigned>(), b->quad.as<double>(),
                                     b->frontier.as<int32_t>(), b->counter.as<unsigned>() + 2,
                                     b->err.as<unsigned>(), s));
-    k_seg_frames<<<(unsigned)ns, kSegThreads, 0, s>>>(
-        b->dev(), b->d_part_off.as<int64_t>(), b->d_node_off.as<int64_t>(), b->box.as<double>(),
-        b->center.as<double>(), b->frames.as<FastFrame>(), b->ph.as<float4>(), b->pl.as<float4>(),
+    k_seg_ff_particles<<<grid_for(n, 256), 256, 0, s>>>(b->dev(), b->sys_of.as<int32_t>(),
+                                                        b->frames.as<FastFrame>(),
+                                                        b->ph.as<float4>(), b->pl.as<float4>());
+    k_seg_ff_nodes<<<grid_for(b->mtot, 256), 256, 0, s>>>(
+        b->dev(), b->node_sys.as<int32_t>(), b->frames.as<FastFrame>(), b->center.as<double>(),
         b->nh.as<float4>(), b->nl.as<float4>(), b->nsize.as<float>(), b->ndelta.as<float>(),
         quad ? b->quad.as<double>() : nullptr, b->nq0.as<float4>(), b->nq1.as<float2>(),
         b->nhdr.as<int4>());
     BHUT_CUDA(cudaGetLastError());
-    note_launches(1);
+    note_launches(2);
     // traversal
     BHUT_CUDA(cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned), s));
     BHUT_CUDA(cudaMemsetAsync(b->stats.p, 0, sizeof(unsigned long long) * 8, s));

@@ -35,18 +35,6 @@ namespace bhut {
 // ---------------------------------------------------------------------------
 constexpr int kBoxThreads = 192;   // a multiple of 6 and of 32
 
-__device__ __forceinline__ uint64_t ord_key(uint64_t b)   // monotone in the double value
-{
-    return b ^ ((uint64_t)((int64_t)b >> 63) | 0x8000000000000000ull);
-}
-__device__ __forceinline__ uint64_t ord_inv(uint64_t k)
-{
-    return k ^ (((k >> 63) ? 0ull : ~0ull) | 0x8000000000000000ull);
-}
-__device__ __forceinline__ bool finite_bits(uint64_t b)
-{
-    return ((b >> 52) & 0x7ff) != 0x7ff;
-}
 
 __global__ void __launch_bounds__(kBoxThreads)
 k_bbox(const double* __restrict__ pos, const double* __restrict__ mass, int64_t n, int dim,

@@ -146,6 +146,22 @@ static __device__ __forceinline__ uint64_t quantise_rcp(double x, double pmin, d
     return k < 2097151ull ? k : 2097151ull;
 }
 
+// Order-preserving integer images of doubles (min/max on the integer pipe,
+// and with 64-bit integer atomics): ord_key(a) < ord_key(b) iff a < b for
+// non-NaN a, b (-0 before +0).
+static __device__ __forceinline__ uint64_t ord_key(uint64_t b)
+{
+    return b ^ ((uint64_t)((int64_t)b >> 63) | 0x8000000000000000ull);
+}
+static __device__ __forceinline__ uint64_t ord_inv(uint64_t k)
+{
+    return k ^ (((k >> 63) ? 0ull : ~0ull) | 0x8000000000000000ull);
+}
+static __device__ __forceinline__ bool finite_bits(uint64_t b)
+{
+    return ((b >> 52) & 0x7ff) != 0x7ff;
+}
+
 static __device__ __forceinline__ uint64_t morton3(uint64_t cx, uint64_t cy, uint64_t cz)
 {
     return expand3(cx) | (expand3(cy) << 1) | (expand3(cz) << 2);
@@ -170,7 +186,8 @@ struct NodeOut {
 // Bounding box: box[0..2] = min, box[3..5] = max, box[6] = max |mass| (0
 // without masses), box[8..10] = RN(1 / (max - min)) per axis (1 for a zero
 // extent), box[11] = 1 if an axis has zero extent, box[12..14] = 1 if the
-// axis holds a NaN.  `partial` holds kBoxPartialDoubles doubles.
+// axis holds a NaN, box[15] = 1 if every mass equals mass[0] > 0 (finite).
+// `partial` holds kBoxPartialDoubles doubles.
 constexpr unsigned kBoxMaxBlocks = 152u * 4u;
 constexpr int kBoxPartialDoubles = 8 * (int)kBoxMaxBlocks;
 constexpr int kBoxDoubles = 16;

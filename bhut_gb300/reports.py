@@ -623,24 +623,39 @@ def precision_record(*, n: int = 4_000_000, n_sample: int = 8192, thetas=(0.3, 0
 
 
 def served_record(*, count: int = 200, rate: float = 200.0, steps: int = 100, seed: int = 21,
-                  server_seconds: float = 45.0, plain_seconds: float = 45.0,
-                  fast_seconds: float = 20.0, solve_budget: int = 2_000_000,
-                  theta: float = 0.7, criterion: str = "bh_offset", multipole: str = "quad",
-                  leaf: int = 16, fast_theta: float = 0.33, err_requests: int = 6,
+                  server_seconds: float = 45.0, full_steps: int = 10, sample_requests: int = 40,
+                  solve_budget: int = 2_000_000, theta: float = 0.7,
+                  criterion: str = "bh_offset", multipole: str = "quad", leaf: int = 16,
+                  fast_theta: float = 0.33, err_requests: int = 6,
                   hbm_budget: float = 150e9) -> dict:
     """The served form on its named stream (Poisson ``rate``/s, N log-uniform
     in [1e3, 2e6], half Plummer half cubes, ``steps`` KDK steps, refit every
-    step, rebuild every 10, HBM budget 150 GB), each leg bounded in wall
-    time: the continuous-batching server (shortest remaining work first
-    within a per-solve particle budget) against the plain per-request path
-    with the same form, theta, criterion, multipole and leaf size (the same
-    arithmetic per system, so equal error by construction) and the same
-    ordering, and against the plain FP64-accurate path (form fast) at a
-    theta whose error vs FP64 direct sum is close to the server's."""
+    step, rebuild every 10, HBM budget 150 GB) against the plain per-request
+    path, in two comparisons:
+
+    * stream: the server runs the open-loop stream in real time for
+      ``server_seconds`` (latency p50/p99 by size class, solves done in the
+      window).  The plain path (one request at a time, shortest work first
+      among the arrived ones, as the server) is scheduled on the same stream
+      and window from its measured per-request costs.
+    * full stream: every request advanced ``full_steps`` steps (a rebuild
+      at the 10th), all queued at t=0: the server's makespan, measured,
+      against the plain path's sum of per-request costs.  In both, solves/s
+      counts every request-step once, whatever its size.
+
+    The plain path's cost of a request (initial solve, refit step, rebuild
+    step; ``serve.plain_service_times``) is measured on ``sample_requests``
+    requests spread over the size range and interpolated in N for the
+    others (leave-one-out error reported).  Two plain configurations: the
+    server's own (form fp32, theta, criterion, multipole, leaf: the same
+    arithmetic per system, equal error by construction -- the ratio isolates
+    batching and residency) and the FP64-accurate form ``fast`` with the
+    reference's criterion at a theta whose error against FP64 direct sums
+    is close to the server's."""
     import dataclasses
     from . import serve
     base = serve.request_stream(count, rate=rate, steps=steps, seed=seed)
-    fresh = lambda: [dataclasses.replace(r) for r in base]  # noqa: E731
+    fresh = lambda k=steps: [dataclasses.replace(r, steps=k) for r in base]  # noqa: E731
     total_n = sum(r.n for r in base)
     by_size = sorted(base, key=lambda r: r.n)
     pick = [by_size[int(round(k))] for k in np.linspace(0, len(by_size) - 1, err_requests)]
@@ -666,12 +681,54 @@ def served_record(*, count: int = 200, rate: float = 200.0, steps: int = 100, se
     sv = serve.Server(**kw, hbm_budget=hbm_budget, solve_budget=solve_budget)
     st = sv.run(fresh(), realtime=True, max_seconds=server_seconds)
     sv.close()
-    pl = serve.plain_path(fresh(), realtime=True, max_seconds=plain_seconds, order="shortest",
-                          **kw)
-    pf = serve.plain_path(fresh(), realtime=True, max_seconds=fast_seconds, order="shortest",
-                          theta=fast_theta, softening=0.01, dt=1e-3, rebuild_every=10,
-                          form="fast", leaf_size=32)
+    sv = serve.Server(**kw, hbm_budget=hbm_budget, solve_budget=solve_budget)
+    full = sv.run(fresh(full_steps), realtime=False)
+    sv.close()
+    full_server = {"solves": full["solves"], "wall_s": full["wall_s"],
+                   "solves_per_s": full["solves_per_s"], "accels_per_s": full["accels_per_s"],
+                   "requests_done": full["requests_done"]}
+
+    spread = [by_size[int(round(k))] for k in np.linspace(0, len(by_size) - 1,
+                                                          min(sample_requests, count))]
+    plain_cfgs = {
+        "plain_same_config": dict(theta=theta, form="fp32", criterion=criterion,
+                                  multipole=multipole, leaf_size=leaf),
+        "plain_fast_equal_error": dict(theta=fast_theta, form="fast", criterion="bh",
+                                       multipole="mono", leaf_size=32),
+    }
+    plain = {}
+    for name, cfg in plain_cfgs.items():
+        t0 = time.perf_counter()
+        meas = serve.plain_service_times(spread, softening=0.01, dt=1e-3, **cfg)
+        t_meas = time.perf_counter() - t0
+        costs = serve.interpolate_service_times(meas, base)
+        loo = []   # leave-one-out: each measured request predicted from the others
+        for k, t in enumerate(meas):
+            rest = meas[:k] + meas[k + 1:]
+            r = next(q for q in base if q.rid == t["rid"])
+            est = serve.interpolate_service_times(rest, [r])[r.rid]
+            c_true = serve.request_cost(t, steps, 10)
+            loo.append(abs(serve.request_cost(est, steps, 10) - c_true) / c_true)
+        full_s = sum(serve.request_cost(costs[r.rid], full_steps, 10) for r in base)
+        window = serve.simulate_sequential(base, costs, steps=steps, rebuild_every=10,
+                                           order="shortest", window=server_seconds)
+        whole = serve.simulate_sequential(base, costs, steps=steps, rebuild_every=10,
+                                          order="shortest")
+        plain[name] = {
+            "config": cfg,
+            "stream_window": window,
+            "stream_to_completion": {k: whole[k] for k in ("wall_s", "solves_per_s",
+                                                           "latency_p50_s", "latency_p99_s",
+                                                           "latency_by_size")},
+            "full_stream": {"solves": count * (full_steps + 1), "wall_s": full_s,
+                            "solves_per_s": count * (full_steps + 1) / full_s},
+            "cost_model": {"requests_measured": len(meas), "measure_s": t_meas,
+                           "loo_rel_err_median": float(np.median(loo)),
+                           "loo_rel_err_max": float(np.max(loo))},
+        }
     ratio = lambda a, b: a / b if b else None  # noqa: E731
+    same, fast = plain["plain_same_config"], plain["plain_fast_equal_error"]
+    work_small = sum(r.n for r in base if r.n < 100_000) / total_n
     return {
         "workload": f"{count} requests ({total_n:,} particles), Poisson {rate:.0f}/s, N "
                     f"log-uniform in [1e3, 2e6], half Plummer half uniform cubes, {steps} KDK "
@@ -681,14 +738,18 @@ def served_record(*, count: int = 200, rate: float = 200.0, steps: int = 100, se
                           "multipole": multipole, "leaf_size": leaf,
                           "scheduling": "shortest remaining work first",
                           "solve_budget_particles": solve_budget},
-        "wall_caps_s": {"server": server_seconds, "plain_same_config": plain_seconds,
-                        "plain_fast": fast_seconds},
-        "server": st,
-        "plain_same_config": pl,
-        "plain_fast_equal_error": pf,
-        "solves_per_s_ratio_vs_same_config": ratio(st["solves_per_s"], pl["solves_per_s"]),
-        "accels_per_s_ratio_vs_same_config": ratio(st["accels_per_s"], pl["accels_per_s"]),
-        "solves_per_s_ratio_vs_fast": ratio(st["solves_per_s"], pf["solves_per_s"]),
+        "server_stream_window": st,
+        "server_full_stream": full_server,
+        "full_stream_steps": full_steps,
+        **plain,
+        "solves_per_s_ratio_full_stream_vs_same_config": ratio(
+            full_server["solves_per_s"], same["full_stream"]["solves_per_s"]),
+        "solves_per_s_ratio_full_stream_vs_fast": ratio(
+            full_server["solves_per_s"], fast["full_stream"]["solves_per_s"]),
+        "solves_in_window_ratio_vs_same_config": ratio(st["solves"],
+                                                       same["stream_window"]["solves"]),
+        "solves_in_window_ratio_vs_fast": ratio(st["solves"], fast["stream_window"]["solves"]),
+        "work_share_of_systems_below_1e5": work_small,
         "median_err_vs_fp64_direct": {
             "server_and_plain_same_config": float(np.median(e_srv)),
             f"plain_fast_theta_{fast_theta}": float(np.median(e_fast)),

@@ -615,3 +615,138 @@ def plain_path(requests: list[Request], *, theta: float = 0.5, softening: float 
             "requests_unfinished": len(pending), "order": order,
             "config": {"form": form, "theta": theta, "criterion": criterion,
                        "multipole": multipole, "leaf_size": leaf_size}}
+
+
+# ---------------------------------------------------------------------------
+# The plain path's cost model (for stream-level comparisons)
+# ---------------------------------------------------------------------------
+def plain_service_times(requests: list[Request], *, theta: float = 0.5, softening: float = 0.01,
+                        G: float = 1.0, dt: float = 1e-3, form: str = "fast",
+                        leaf_size: int = 32, criterion: str = "bh",
+                        multipole: str = "mono") -> list[dict]:
+    """Measures what each request costs the plain per-request path (one
+    ``Tree`` per request, as ``plain_path``): the initial solve (build +
+    accelerations), one refit step and one rebuild step (half kick, drift,
+    refit or rebuild, accelerations, half kick), each timed as host wall
+    time with the device synchronised before and after.  The path runs one
+    request at a time, so a request's cost does not depend on the others."""
+    import torch
+    L = _lib.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    out = []
+    for r in requests:
+        x = torch.as_tensor(np.asarray(r.positions), device="cuda").clone()
+        v = torch.as_tensor(np.asarray(r.velocities), device="cuda").clone()
+        m = torch.as_tensor(np.asarray(r.masses), device="cuda").clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tree = api.Tree(x, m, leaf_size=leaf_size, form=form, criterion=criterion,
+                        multipole=multipole).build()
+        a = tree.accelerations(theta=theta, softening=softening, G=G)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        times = []
+        for rebuild in (False, True):
+            _leapfrog(L, x, v, a, r.n, 0.5 * dt, dt, stream)
+            if rebuild:
+                tree.rebuild(x, m)
+            else:
+                tree.refit(x, m)
+            a = tree.accelerations(theta=theta, softening=softening, G=G)
+            _leapfrog(L, x, v, a, r.n, 0.5 * dt, 0.0, stream)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            times.append(t2 - t1)
+            t1 = t2
+        tree.close()
+        out.append({"rid": r.rid, "n": r.n, "kind": r.kind, "t_prime": t1 - t0 - sum(times),
+                    "t_refit": times[0], "t_rebuild": times[1]})
+    return out
+
+
+def request_cost(t: dict, steps: int, rebuild_every: int) -> float:
+    """Plain-path seconds for one request of ``steps`` steps from its
+    measured per-step costs (a rebuild every ``rebuild_every`` steps)."""
+    rebuilds = steps // rebuild_every
+    return t["t_prime"] + rebuilds * t["t_rebuild"] + (steps - rebuilds) * t["t_refit"]
+
+
+def interpolate_service_times(measured: list[dict], requests: list[Request]) -> dict:
+    """Per-request costs for every request: measured ones as they are, the
+    others interpolated log-log in N between measured requests of the same
+    kind (beyond the measured range: the nearest end, scaled in proportion
+    to N above it).  Returns {rid: times}."""
+    by_kind: dict[str, list[dict]] = {}
+    for t in measured:
+        by_kind.setdefault(t["kind"], []).append(t)
+    known = {t["rid"]: t for t in measured}
+    out = {}
+    for r in requests:
+        if r.rid in known:
+            out[r.rid] = known[r.rid]
+            continue
+        pts = sorted(by_kind.get(r.kind) or measured, key=lambda t: t["n"])
+        ln = np.log([t["n"] for t in pts])
+        est = {"rid": r.rid, "n": r.n, "kind": r.kind, "interpolated": True}
+        for key in ("t_prime", "t_refit", "t_rebuild"):
+            lt = np.log([max(t[key], 1e-9) for t in pts])
+            x = np.log(r.n)
+            if x > ln[-1]:
+                v = float(np.exp(lt[-1]) * r.n / pts[-1]["n"])
+            else:
+                v = float(np.exp(np.interp(x, ln, lt)))
+            est[key] = v
+        out[r.rid] = est
+    return out
+
+
+def simulate_sequential(requests: list[Request], costs: dict, *, steps: int,
+                        rebuild_every: int, order: str = "shortest",
+                        window: float | None = None) -> dict:
+    """The plain path's schedule on a stream from per-request costs: one
+    request at a time; when one finishes, the next is, of the requests that
+    have arrived, the one with the least work (``order="shortest"``, the
+    server's ordering) or the earliest.  ``window``: only what completes by
+    then counts (a request in progress contributes the solves it finished).
+    Returns the same summary fields as ``Server.run``."""
+    pending = sorted(requests, key=lambda r: r.arrival)
+    t = 0.0
+    done = []
+    solves = 0
+    accels = 0
+    while pending:
+        if window is not None and t >= window:
+            break
+        arrived = [r for r in pending if r.arrival <= t]
+        if not arrived:
+            t = pending[0].arrival
+            continue
+        r = (min(arrived, key=lambda q: (q.n * q.steps, q.rid)) if order == "shortest"
+             else arrived[0])
+        pending.remove(r)
+        c = costs[r.rid]
+        dur = request_cost(c, steps, rebuild_every)
+        if window is not None and t + dur > window:
+            # partial: the initial solve, then whole steps at the mean step cost
+            left = window - t - c["t_prime"]
+            if left >= 0:
+                per = dur - c["t_prime"]
+                k = min(steps, int(left / (per / steps))) if per > 0 else steps
+                solves += 1 + k
+                accels += r.n * (1 + k)
+            t = window
+            break
+        t += dur
+        solves += steps + 1
+        accels += r.n * (steps + 1)
+        done.append((r, t))
+    wall = t if window is None else window
+    lat = [(r.n, end - r.arrival) for r, end in done]
+    arr = np.array([x for _, x in lat])
+    return {"requests_done": len(done), "wall_s": wall, "solves": solves,
+            "solves_per_s": solves / wall if wall else 0.0,
+            "accels_per_s": accels / wall if wall else 0.0,
+            "latency_p50_s": float(np.percentile(arr, 50)) if arr.size else None,
+            "latency_p99_s": float(np.percentile(arr, 99)) if arr.size else None,
+            "latency_by_size": latency_summary(lat),
+            "requests_unfinished": len(requests) - len(done), "order": order}

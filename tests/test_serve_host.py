@@ -87,3 +87,47 @@ def test_latency_summary_by_size_class():
     assert s["1e4<=n<1e5"]["p99_s"] == 10.0
     assert s["n>=1e5"]["count"] == 1
     assert serve.latency_summary([])["all"]["p50_s"] is None
+
+
+def _req(rid, arrival, n, kind="plummer", steps=10):
+    z = np.zeros((n, 3))
+    return serve.Request(rid, arrival, z, z, np.ones(n), steps=steps, kind=kind)
+
+
+def test_plain_request_cost_from_step_costs():
+    t = {"t_prime": 1.0, "t_refit": 0.1, "t_rebuild": 0.3}
+    assert np.isclose(serve.request_cost(t, 100, 10), 1.0 + 10 * 0.3 + 90 * 0.1)
+    assert np.isclose(serve.request_cost(t, 10, 10), 1.0 + 0.3 + 9 * 0.1)
+
+
+def test_service_time_interpolation():
+    meas = [{"rid": 0, "n": 1000, "kind": "plummer", "t_prime": 1e-3, "t_refit": 1e-3,
+             "t_rebuild": 2e-3},
+            {"rid": 1, "n": 100_000, "kind": "plummer", "t_prime": 1e-1, "t_refit": 1e-1,
+             "t_rebuild": 2e-1}]
+    reqs = [_req(0, 0.0, 1000), _req(2, 0.0, 10_000), _req(3, 0.0, 200_000), _req(4, 0.0, 500)]
+    c = serve.interpolate_service_times(meas, reqs)
+    assert c[0] is meas[0]
+    assert np.isclose(c[2]["t_refit"], 1e-2) and np.isclose(c[2]["t_rebuild"], 2e-2)
+    assert np.isclose(c[3]["t_refit"], 2e-1)           # beyond: in proportion to N
+    assert np.isclose(c[4]["t_refit"], 1e-3)           # below: the nearest end
+
+
+def test_sequential_schedule_shortest_first_and_window():
+    reqs = [_req(0, 0.0, 100), _req(1, 0.5, 100), _req(2, 0.6, 10)]
+    costs = {0: {"t_prime": 0.0, "t_refit": 0.1, "t_rebuild": 0.1},
+             1: {"t_prime": 0.0, "t_refit": 0.1, "t_rebuild": 0.1},
+             2: {"t_prime": 0.0, "t_refit": 0.02, "t_rebuild": 0.02}}
+    s = serve.simulate_sequential(reqs, costs, steps=10, rebuild_every=10, order="shortest")
+    # r0 runs 0..1; then r2 (less work) 1..1.2; then r1 1.2..2.2
+    assert s["requests_done"] == 3 and np.isclose(s["wall_s"], 2.2)
+    assert s["solves"] == 33
+    lat = sorted([1.0, 1.2 - 0.6, 2.2 - 0.5])
+    assert np.isclose(s["latency_by_size"]["all"]["p50_s"], np.percentile(lat, 50))
+    f = serve.simulate_sequential(reqs, costs, steps=10, rebuild_every=10, order="arrival")
+    assert np.isclose(f["wall_s"], 2.2) and f["requests_done"] == 3
+    w = serve.simulate_sequential(reqs, costs, steps=10, rebuild_every=10, order="shortest",
+                                  window=1.1)
+    # r0 done; r2 started at 1.0 and finished 5 of its 10 steps (plus its first solve)
+    assert w["requests_done"] == 1 and w["solves"] == 11 + 1 + 5
+    assert np.isclose(w["wall_s"], 1.1)
