@@ -401,7 +401,7 @@ def run_ours(args, ws, rank, local):
         else:
             from bhut_gb300 import reports
             ops = reports.fp32_ops(p2p, m2p, "mono")
-            rule = (f"{reports.F32_OPS_PER_PAIR} FP32 ops per pair term, "
+            rule = (f"{reports.F32_OPS_PER_PAIR} FP32 ops per pair term (unit-mass frame), "
                     f"{reports.F32_OPS_PER_MONOPOLE} per Kahan-added monopole")
         achieved32 = ops / trav_s / 1e12
         # FP32 pipe lane-instructions per second (one FMA = 2 flop): the FMA

@@ -623,6 +623,8 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                 z = DIM == 3 ? t.sz[i] : 0.0;
             }
         }
+        const TargetF32x2 tx = target_f32x2(Th, Tl);
+        const bool unit = fr.unit != 0;   // every particle mass of this system exactly 1
         float ah[3] = {0.f, 0.f, 0.f}, al[3] = {0.f, 0.f, 0.f};   // ff sum, or (sum, Kahan comp)
         double a64[3] = {0.0, 0.0, 0.0};
         unsigned cnt[5] = {0, 0, 0, 0, 0};
@@ -652,22 +654,33 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                     if (act) {
                         if (sub == 0) cnt[0] += cn - (i >= s0 + bb && i < s0 + bb + cn);
                         if (FP32) {   // <= 32 terms in FP32, then one Kahan step
-                            float part[3] = {0.f, 0.f, 0.f};
-                            if (soft) {
+                            float2 pxy = make_float2(0.f, 0.f);
+                            float pz = 0.f;
+                            if (soft && unit) {
 #pragma unroll 8
                                 for (int q = sub; q < cn; q += LPT)
-                                    pair_f32_partial<DIM, false>(Th, Tl, sh[w][q], sl[w][q], e2h,
-                                                                 part);
+                                    pair_f32_partial2<DIM, false, true>(tx, sh[w][q], sl[w][q],
+                                                                        e2h, pxy, pz);
+                            } else if (soft) {
+#pragma unroll 8
+                                for (int q = sub; q < cn; q += LPT)
+                                    pair_f32_partial2<DIM, false, false>(tx, sh[w][q], sl[w][q],
+                                                                         e2h, pxy, pz);
                             } else {
 #pragma unroll 8
                                 for (int q = sub; q < cn; q += LPT)
-                                    pair_f32_partial<DIM, true>(Th, Tl, sh[w][q], sl[w][q], e2h,
-                                                                part);
+                                    pair_f32_partial2<DIM, true, false>(tx, sh[w][q], sl[w][q],
+                                                                        e2h, pxy, pz);
                             }
+                            const float part[3] = {pxy.x, pxy.y, pz};
                             kahan_add_f32<DIM>(part, ah, al);
                         } else {
                             unsigned fb = 0;   // pairs left to FP64, taken after the loop
-                            if (soft) {
+                            if (soft && unit) {
+                                for (int q = sub; q < cn; q += LPT)
+                                    pair_ff_soft<DIM, true>(Th, Tl, sh[w][q], sl[w][q], e2h, e2l,
+                                                            ah, al);
+                            } else if (soft) {
                                 for (int q = sub; q < cn; q += LPT)
                                     pair_ff_soft<DIM, false>(Th, Tl, sh[w][q], sl[w][q], e2h, e2l,
                                                              ah, al);

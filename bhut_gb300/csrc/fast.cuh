@@ -349,6 +349,46 @@ __device__ __forceinline__ void pair_f32_partial(const float* Th, const float* T
     if (DIM == 3) p[2] = fmaf(f, d2, p[2]);
 }
 
+// A target's negated hi and lo coordinates, x and y packed for the f32x2
+// instructions of pair_f32_partial2.
+struct TargetF32x2 {
+    float2 hxy, lxy;
+    float hz, lz;
+};
+
+static __device__ __forceinline__ TargetF32x2 target_f32x2(const float* T, const float* Tl)
+{
+    TargetF32x2 t;
+    t.hxy = make_float2(-T[0], -T[1]);
+    t.lxy = make_float2(-Tl[0], -Tl[1]);
+    t.hz = -T[2];
+    t.lz = -Tl[2];
+    return t;
+}
+
+// pair_f32_partial with the x and y components in Blackwell's f32x2
+// instructions (FADD2 / FFMA2: two IEEE single operations per issue slot).
+// Every operation and its order are those of pair_f32_partial (x - y is
+// x + (-y) exactly), so the result is the same bit for bit.  UNIT: the
+// source's mass is exactly 1 (the unit-mass frame) and the product with it
+// is skipped, also exactly.
+template <int DIM, bool CHECK, bool UNIT>
+__device__ __forceinline__ void pair_f32_partial2(const TargetF32x2& t, float4 sh, float4 sl,
+                                                  float e2, float2& pxy, float& pz)
+{
+    const float2 dxy = __fadd2_rn(__fadd2_rn(make_float2(sh.x, sh.y), t.hxy),
+                                  __fadd2_rn(make_float2(sl.x, sl.y), t.lxy));
+    const float dz = DIM == 3 ? __fadd_rn(__fadd_rn(sh.z, t.hz), __fadd_rn(sl.z, t.lz)) : 0.0f;
+    float r2 = fmaf(dxy.y, dxy.y, fmaf(dxy.x, dxy.x, e2));
+    if (DIM == 3) r2 = fmaf(dz, dz, r2);
+    const bool ok = !CHECK || r2 >= 0x1p-126f;
+    const float ri = rsqrt_mufu(ok ? r2 : 1.0f);
+    const float w = ri * ri * ri;
+    const float f = ok ? (UNIT ? w : sh.w * w) : 0.0f;
+    pxy = __ffma2_rn(make_float2(f, f), dxy, pxy);
+    if (DIM == 3) pz = fmaf(f, dz, pz);
+}
+
 template <int DIM>
 __device__ __forceinline__ void kahan_add_f32(const float* p, float* acc, float* cmp)
 {

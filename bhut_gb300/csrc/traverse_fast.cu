@@ -386,6 +386,8 @@ __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, c
     const unsigned FULL = 0xffffffffu;
     const float theta_f = (float)a.theta;
     const bool soft = a.e2h >= 0x1p-126f;   // r^2 >= eps^2 is normal: no small-r test
+    const bool unit = ft.frame->unit != 0;   // every particle mass exactly 1
+    const TargetF32x2 tx = target_f32x2(T, Tl);
     const unsigned live = __ballot_sync(FULL, valid);
     if (lane == 0) stack[w][0] = make_int2(0, (int)live);
     int sp = 1;
@@ -412,16 +414,25 @@ __device__ __forceinline__ void walk_f32(const TreeDev& t, const FastTree& ft, c
                 const int cn = min(kWarp, c - b);
                 if (act) {
                     cnt[0] += cn - (me_sorted >= s + b && me_sorted < s + b + cn);
-                    float part[3] = {0.f, 0.f, 0.f};   // <= 32 terms, then one Kahan step
-                    if (soft) {
+                    float2 pxy = make_float2(0.f, 0.f);   // <= 32 terms, then one Kahan step
+                    float pz = 0.f;
+                    if (soft && unit) {
 #pragma unroll (kF32Unroll)
                         for (int q = 0; q < cn; q++)
-                            pair_f32_partial<DIM, false>(T, Tl, sh[w][q], sl[w][q], a.e2h, part);
+                            pair_f32_partial2<DIM, false, true>(tx, sh[w][q], sl[w][q], a.e2h,
+                                                                pxy, pz);
+                    } else if (soft) {
+#pragma unroll (kF32Unroll)
+                        for (int q = 0; q < cn; q++)
+                            pair_f32_partial2<DIM, false, false>(tx, sh[w][q], sl[w][q], a.e2h,
+                                                                 pxy, pz);
                     } else {
 #pragma unroll (kF32Unroll)
                         for (int q = 0; q < cn; q++)
-                            pair_f32_partial<DIM, true>(T, Tl, sh[w][q], sl[w][q], a.e2h, part);
+                            pair_f32_partial2<DIM, true, false>(tx, sh[w][q], sl[w][q], a.e2h,
+                                                                pxy, pz);
                     }
+                    const float part[3] = {pxy.x, pxy.y, pz};
                     kahan_add_f32<DIM>(part, acc, cmp);
                 }
                 __syncwarp();

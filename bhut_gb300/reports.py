@@ -362,13 +362,15 @@ def build_report(n: int = 1_000_000, reps: int = 10, leaf: int = 32, seed: int =
 # Sub-records of the benchmark line (bench.py): each bounded in time
 # ---------------------------------------------------------------------------
 # FP32-pipe operations per evaluation, counted from bhut_gb300/csrc/fast.cuh:
-# a pair term into a leaf partial (pair_f32_partial: displacement 9,
-# r^2 + eps^2 3, cube 2, m * w 1, three FMAs 3), a Kahan-added monopole
-# (pair_f32: the same 15 plus a Kahan step per component 12), a Kahan-added
-# monopole + quadrupole node (node_quad_f32: displacement 9, r^2 3, powers 3,
-# Q d 9, d.Q d 3, force factor 4, per component 6 -> 49), each plus one MUFU
-# rsqrt.
-F32_OPS_PER_PAIR = 18
+# a pair term into a leaf partial (pair_f32_partial2: displacement 9,
+# r^2 + eps^2 3, cube 2, m * w 1 -- none in the unit-mass frame -- three
+# FMAs 3; the x and y operations run as f32x2 instructions, two operations
+# per issue), a Kahan-added monopole (pair_f32: the same 15 plus a Kahan step
+# per component 12), a Kahan-added monopole + quadrupole node (node_quad_f32:
+# displacement 9, r^2 3, powers 3, Q d 9, d.Q d 3, force factor 4, per
+# component 6 -> 49), each plus one MUFU rsqrt.  Every workload here has
+# equal masses (the unit-mass frame).
+F32_OPS_PER_PAIR = 17
 F32_OPS_PER_MONOPOLE = 27
 F32_OPS_PER_QUAD_NODE = 49
 
@@ -386,9 +388,9 @@ def fp32_roofline(ops: int, seconds: float, fma_rate: float, kernel: str, multip
     return {"bound": "fp32", "kernel": kernel, "achieved": achieved, "peak": fma_rate,
             "unit": "T FP32-pipe ops/s", "frac": achieved / fma_rate,
             "work_per_launch": int(ops),
-            "work_rule": f"{F32_OPS_PER_PAIR} FP32 ops per pair term, {node} per "
-                         f"{'monopole+quadrupole' if multipole == 'quad' else 'monopole'} node, "
-                         "x evaluations counted by the kernel",
+            "work_rule": f"{F32_OPS_PER_PAIR} FP32 ops per pair term (unit-mass frame), {node} "
+                         f"per {'monopole+quadrupole' if multipole == 'quad' else 'monopole'} "
+                         "node, x evaluations counted by the kernel",
             "peak_source": "independent FP32 FMA chains on every SM, measured in this run"}
 
 
