@@ -56,7 +56,14 @@ inline unsigned grid_for(int64_t n, int block, unsigned cap = 152u * 16u)
 // Radix sort of (uint64 key, int32 value) pairs, stable, LSD, 8-bit digits
 // (sort.cu).
 // ---------------------------------------------------------------------------
-constexpr int kSortTile = 4096;        // keys per tile (8 warps x 512)
+// Keys per tile: 2^BHUT_SORT_TILE_SHIFT (8 warps x 256 keys by default).
+// Smaller tiles give more blocks for the latency-bound rank/scatter step at
+// moderate n, at the price of larger count tables.
+#ifndef BHUT_SORT_TILE_SHIFT
+#define BHUT_SORT_TILE_SHIFT 11
+#endif
+constexpr int kSortTileShift = BHUT_SORT_TILE_SHIFT;
+constexpr int kSortTile = 1 << kSortTileShift;
 constexpr int kSortThreads = 256;
 constexpr int kSortPassesMax = 8;      // 64 key bits
 

@@ -13,7 +13,7 @@
 // Limits and sharing:
 //  * at most kNoAllocMaxPoints points per call (the array is sized for it);
 //    larger requests are rejected with BHUT_EINVAL;
-//  * the array (about 12.9 MB) is held on every GPU that loads this library
+//  * the array (about 13.7 MB) is held on every GPU that loads this library
 //    until the process exits;
 //  * every call uses the same array and leaves its contents behind; the
 //    counters that must start at zero are cleared at the start of each call.

@@ -33,12 +33,15 @@ namespace bhut {
 
 namespace {
 
-constexpr int kItems = kSortTile / kSortThreads;       // 16 keys per thread
+constexpr int kItems = kSortTile / kSortThreads;       // keys per thread
 constexpr int kWarpsPerTile = kSortThreads / kWarp;    // 8
-constexpr int kWarpSpan = kSortTile / kWarpsPerTile;   // 512 keys per warp
+constexpr int kWarpSpan = kSortTile / kWarpsPerTile;   // keys per warp
 constexpr int kScanThreads = 256;
-constexpr int kTileShift = 12;                          // log2(kSortTile)
-static_assert((1 << kTileShift) == kSortTile, "tile size must be 2^kTileShift");
+constexpr int kTileShift = kSortTileShift;             // log2(kSortTile)
+static_assert(kItems >= 1 && kItems * kSortThreads == kSortTile, "tile of whole warps");
+// resident scatter blocks per SM the register budget must allow (shared
+// memory allows three 59 KB tiles of 4,096 keys, five 34 KB tiles of 2,048)
+constexpr int kScatterMinBlocks = kSortTileShift >= 12 ? 3 : 4;
 static_assert(kScanThreads == kSortThreads, "the scan helper serves both kernels");
 
 __device__ __forceinline__ int64_t item_pos(int64_t tile, int warp, int item, int lane)
@@ -158,7 +161,7 @@ k_sort_scan(uint32_t* __restrict__ counts, int64_t tiles, const uint32_t* __rest
 
 // k_sort_scatter: see the file comment.  `next_counts` (may be null) gets
 // the digit at `next_shift` of every key, per destination tile.
-__global__ void __launch_bounds__(kSortThreads, 3)
+__global__ void __launch_bounds__(kSortThreads, kScatterMinBlocks)
 k_sort_scatter(const uint64_t* __restrict__ keys_in, const int32_t* __restrict__ vals_in,
                uint64_t* __restrict__ keys_out, int32_t* __restrict__ vals_out, int64_t n,
                int shift, const uint32_t* __restrict__ offsets, int64_t tiles,
@@ -288,8 +291,8 @@ int radix_sort_pairs(uint64_t* keys, int32_t* vals, int64_t n, int bits, void* s
             BHUT_CUDA(cudaFuncSetAttribute(k_sort_scatter,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)sizeof(ScatterSmem)));
-            // all of the unified L1/shared storage as shared memory: three
-            // 59 KB tiles per SM
+            // all of the unified L1/shared storage as shared memory (several
+            // tiles per SM)
             BHUT_CUDA(cudaFuncSetAttribute(k_sort_scatter,
                                            cudaFuncAttributePreferredSharedMemoryCarveout,
                                            (int)cudaSharedmemCarveoutMaxShared));

@@ -149,7 +149,7 @@ BHUT_API int bhut_morton_argsort(const double *positions, int64_t n, int dim, ui
  * allocation would synchronize the device).  Same result as
  * bhut_morton_argsort, with perm as int32.  All pointers must be memory of
  * the current device (or managed memory); n <= 1,048,576.  Scratch is one
- * static device array (about 12.9 MB, held on every GPU that loads the
+ * static device array (about 13.7 MB, held on every GPU that loads the
  * library until exit) shared by all calls: calls that overlap on the GPU
  * race.  The first call on a device looks up the array's address; make it
  * before any stream capture, and make no call after cudaDeviceReset.  Each
