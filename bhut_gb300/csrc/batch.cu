@@ -651,8 +651,15 @@ k_batch_traverse(BatchDev b, BatchArgs a)
                     }
                     __syncwarp();
                     const int cn = min(kWarp, c - bb);
-                    if (act) {
-                        if (sub == 0) cnt[0] += cn - (i >= s0 + bb && i < s0 + bb + cn);
+                    if (act && sub == 0) cnt[0] += cn - (i >= s0 + bb && i < s0 + bb + cn);
+                    if (!FP32 && LPT == 1 && soft) {   // as the single-tree walk
+                        if (unit)
+                            leaf_block_soft<DIM, true>((unsigned)e.y, lane, Th, Tl, sh[w], sl[w],
+                                                       cn, e2h, e2l, ah, al);
+                        else
+                            leaf_block_soft<DIM, false>((unsigned)e.y, lane, Th, Tl, sh[w], sl[w],
+                                                        cn, e2h, e2l, ah, al);
+                    } else if (act) {
                         if (FP32) {   // <= 32 terms in FP32, then one Kahan step
                             float2 pxy = make_float2(0.f, 0.f);
                             float pz = 0.f;

@@ -11,8 +11,31 @@
 #ifndef BHUT_FF_KNUTH_ACC
 #define BHUT_FF_KNUTH_ACC 0
 #endif
+// Unroll factor of the float-float leaf pair loops (swept on GB300 at 1M
+// Plummer: 4 beats 1-2 by 2-10 %).
+#ifndef BHUT_FF_UNROLL
+#define BHUT_FF_UNROLL 4
+#endif
 
 namespace bhut {
+
+constexpr int kFFUnroll = BHUT_FF_UNROLL;
+// leaf_block_soft: leaf visits with at most BHUT_SPLIT_MAXK active lanes are
+// split across the idle lanes; the split pair loop is unrolled
+// BHUT_SPLIT_UNROLL times.  Swept on GB300 at 1M Plummer (theta 0.5, leaf
+// 32): split at <= 16 active lanes 173.8 ms, at <= 8 178.9 ms, no split
+// 187.2 ms; split-loop unroll 2 173.8 ms, 1 174.0 ms, 4 175.7 ms.  The FP32
+// form's pair term is too cheap for the split to pay (63.9-64.1 ms against
+// 62.7 ms unsplit), so it keeps one lane per target.
+#ifndef BHUT_SPLIT_MAXK
+#define BHUT_SPLIT_MAXK 16
+#endif
+#ifndef BHUT_SPLIT_UNROLL
+#define BHUT_SPLIT_UNROLL 2
+#endif
+constexpr int kSplitMaxK = BHUT_SPLIT_MAXK;
+constexpr int kSplitUnroll = BHUT_SPLIT_UNROLL;
+static_assert(kSplitMaxK <= 16, "a split gives every active target at least two lanes");
 
 // r^2 + eps^2 below this (normalised units) -> FP64 pair.  The coordinates
 // are represented to 2^-48, so a pair's relative error is about
@@ -255,6 +278,103 @@ __device__ __forceinline__ void pair_ff_soft(const float* Th, const float* Tl, f
 #endif
         ah[k] = t;
         al[k] = __fadd_rn(al[k], __fadd_rn(err, Fl));
+    }
+}
+
+// Float-float (ah, al) += (bh, bl): TwoSum of the high parts, the low parts
+// added to its error, renormalised by FastTwoSum.
+static __device__ __forceinline__ void ff_add(float& ah, float& al, float bh, float bl)
+{
+    const float s = __fadd_rn(ah, bh);
+    const float e = __fadd_rn(two_sum_err(ah, bh, s), __fadd_rn(al, bl));
+    const float h = __fadd_rn(s, e);
+    al = __fsub_rn(e, __fsub_rn(h, s));
+    ah = h;
+}
+
+// Position of the set bit of rank r (0-based, from the least significant
+// bit) of m; m must have more than r bits set.
+static __device__ __forceinline__ int nth_set_bit(unsigned m, int r)
+{
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const int c = __popc(m & ((1u << w) - 1u));
+        if (r >= c) {
+            r -= c;
+            m >>= w;
+            pos += w;
+        }
+    }
+    return pos;
+}
+
+// One block of cn <= 32 leaf particles, staged in sh/sl, for the targets of
+// the lanes in `mask` (those that opened the leaf's parent), float-float
+// soft path (pair_ff_soft).  Called by all 32 lanes.
+//
+// With more than 16 active lanes each lane adds its pairs in order to its
+// accumulator.  With k <= 16 active lanes the idle lanes are put to work:
+// every active target gets f lanes (f = 2..32, the largest power of two with
+// f k <= 32); lane j works for the active target of rank j / f, on the pairs
+// q = j mod f, j mod f + f, ..., into a float-float partial sum that starts
+// at zero; the f partials are added in a fixed tree order (shuffles down by
+// f/2, f/4, ..., 1) and the group's sum is added to the target's
+// accumulator with ff_add.  Leaf visits with at most 16 active lanes carry
+// most of the warp's idle lanes (a CPU replay of the walk at 1M Plummer,
+// theta 0.5, leaf 32: 16 % of the leaf steps, 84 % of the idle lane-steps),
+// and the split cuts the pair steps of a solve by about a tenth.  The order
+// of every addition depends only on the mask and cn, so a result does not
+// depend on which kernel (single tree or batched) evaluates it.
+template <int DIM, bool UNIT>
+__device__ __forceinline__ void leaf_block_soft(unsigned mask, int lane, const float* Th,
+                                                const float* Tl, const float4* sh,
+                                                const float4* sl, int cn, float e2h, float e2l,
+                                                float* ah, float* al)
+{
+    const unsigned FULL = 0xffffffffu;
+    const bool mine = (mask >> lane) & 1u;
+    const int k = __popc(mask);
+    if (k == 0) return;
+    if (k > kSplitMaxK) {
+        if (mine) {
+#pragma unroll (kFFUnroll)
+            for (int q = 0; q < cn; q++)
+                pair_ff_soft<DIM, UNIT>(Th, Tl, sh[q], sl[q], e2h, e2l, ah, al);
+        }
+        return;
+    }
+    int f = 2;
+    while (f * 2 * k <= kWarp) f *= 2;
+    const int r = lane / f, sub = lane & (f - 1);
+    const bool work = r < k;
+    const int owner = nth_set_bit(mask, work ? r : 0);
+    float T[3] = {0.f, 0.f, 0.f}, L[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+        T[c] = __shfl_sync(FULL, Th[c], owner);
+        L[c] = __shfl_sync(FULL, Tl[c], owner);
+    }
+    float ph[3] = {0.f, 0.f, 0.f}, pl[3] = {0.f, 0.f, 0.f};
+    if (work) {
+#pragma unroll (kSplitUnroll)
+        for (int q = sub; q < cn; q += f)
+            pair_ff_soft<DIM, UNIT>(T, L, sh[q], sl[q], e2h, e2l, ph, pl);
+    }
+    for (int o = f >> 1; o >= 1; o >>= 1) {
+#pragma unroll
+        for (int c = 0; c < DIM; c++) {
+            const float bh = __shfl_down_sync(FULL, ph[c], o);
+            const float bl = __shfl_down_sync(FULL, pl[c], o);
+            ff_add(ph[c], pl[c], bh, bl);
+        }
+    }
+    const int leader = mine ? __popc(mask & ((1u << lane) - 1u)) * f : 0;
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+        const float gh = __shfl_sync(FULL, ph[c], leader);
+        const float gl = __shfl_sync(FULL, pl[c], leader);
+        if (mine) ff_add(ah[c], al[c], gh, gl);
     }
 }
 

@@ -42,14 +42,10 @@ constexpr int kFastThreads = kFastWarps * kWarp;
 #ifndef BHUT_FAST_BLOCKS
 #define BHUT_FAST_BLOCKS 6
 #endif
-#ifndef BHUT_FF_UNROLL
-#define BHUT_FF_UNROLL 4
-#endif
 #ifndef BHUT_F32_UNROLL
 #define BHUT_F32_UNROLL 8
 #endif
 constexpr int kFastBlocksPerSM = BHUT_FAST_BLOCKS;
-constexpr int kFFUnroll = BHUT_FF_UNROLL;
 constexpr int kF32Unroll = BHUT_F32_UNROLL;
 
 // ---------------------------------------------------------------------------
@@ -218,18 +214,16 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                     // is not skipped; it is only left out of the pair count
                     // (bh.py:254).
                     cnt[0] += cn - (me_sorted >= s + b && me_sorted < s + b + cn);
+                }
+                if (!FAR && !CHECK) {
+                    leaf_block_soft<DIM, UNIT>(mask, lane, Th, Tl, sh[w], sl[w], cn, a.e2h, a.e2l,
+                                               ah, al);
+                } else if (act) {
                     unsigned fb = 0;   // pairs left to FP64 (rare), taken after the loop
-                    if (!FAR && !CHECK) {
 #pragma unroll (kFFUnroll)
-                        for (int q = 0; q < cn; q++)
-                            pair_ff_soft<DIM, UNIT>(Th, Tl, sh[w][q], sl[w][q], a.e2h, a.e2l, ah,
-                                                    al);
-                    } else {
-#pragma unroll (kFFUnroll)
-                        for (int q = 0; q < cn; q++)
-                            fb |= (unsigned)!pair_ff<DIM, FAR, CHECK>(Th, Tl, sh[w][q], sl[w][q],
-                                                                      a.e2h, a.e2l, ah, al) << q;
-                    }
+                    for (int q = 0; q < cn; q++)
+                        fb |= (unsigned)!pair_ff<DIM, FAR, CHECK>(Th, Tl, sh[w][q], sl[w][q],
+                                                                  a.e2h, a.e2l, ah, al) << q;
                     while (fb) {
                         const int gi = s + b + __ffs(fb) - 1;
                         fb &= fb - 1;
