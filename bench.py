@@ -469,6 +469,9 @@ def run_ours(args, ws, rank, local):
         if not args.no_c1:
             c1 = reports.c1_record(fma_rate=fma_rate)
             line["c1"] = c1[0]
+        if not args.no_c2_sequence:
+            line["c2_sequence"] = reports.c2_sequence_record(pos_d, m_d, theta=THETA, eps=EPS,
+                                                             G=G, leaf=LEAF)
         if not args.no_exact:
             line["exact"] = reports.exact_record(pos_d, m_d, theta=THETA, eps=EPS, G=G,
                                                  leaf=LEAF, fp64_peak=peak64)
@@ -529,6 +532,8 @@ def main():
     ap.add_argument("--quick", action="store_true",
                     help="headline only: no exact, batched, precision or served sub-record")
     ap.add_argument("--no-exact", action="store_true")
+    ap.add_argument("--no-c2-sequence", action="store_true",
+                    help="skip the external-target / refit / rebuild record of the 1M workload")
     ap.add_argument("--no-c1", action="store_true",
                     help="skip the 10,000-particle Gaussian sub-record")
     ap.add_argument("--no-batched", action="store_true")

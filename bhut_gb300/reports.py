@@ -433,6 +433,63 @@ def exact_record(pos_d, m_d, *, theta: float, eps: float, G: float, leaf: int,
             "interactions_per_solve": {"p2p": p2p, "m2p": m2p, "node_visits": visits}}
 
 
+def c2_sequence_record(pos_d, m_d, *, theta: float, eps: float, G: float, leaf: int,
+                       n_targets: int = 250_000, reps: int = 3) -> dict:
+    """The rest of the 1M Plummer sequence, form "fast", through one tree
+    handle (bhut.Tree): accelerations at external targets uniform in a
+    centred cube of side 10, then a refit after positions += 0.01 N(0, 1)
+    (bhut/tree/refit.py: refit, or a rebuild when a particle left 1.1x the
+    root box) followed by a self solve, then a rebuild of the moved particles
+    followed by a self solve.  Each step's device time by CUDA events on the
+    handle's stream, median of ``reps``, inputs resident on the device."""
+    import torch
+    from .api import _Handle
+    n = int(pos_d.shape[0])
+    tg = torch.as_tensor(workloads.cube_targets(n_targets, seed=5, side=10.0)).cuda()
+    gen = torch.Generator(device="cuda").manual_seed(6)
+    moved = pos_d + 0.01 * torch.randn(pos_d.shape, dtype=pos_d.dtype, device="cuda",
+                                       generator=gen)
+    stream = torch.cuda.Stream()
+    h = _Handle(3, leaf, stream=stream.cuda_stream)
+    h.set_form("fast")
+    out_t = torch.empty((n_targets, 3), dtype=torch.float64, device="cuda")
+    out = torch.empty_like(pos_d)
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r = fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        ts.sort()
+        return ts[len(ts) // 2], r
+
+    h.build(pos_d, m_d)
+    h.accel_targets(tg, theta, eps, G, out_t)          # first call: target buffers
+    t_tg, _ = timed(lambda: h.accel_targets(tg, theta, eps, G, out_t))
+    p2p_t, m2p_t, _ = h.stats()
+    # refit of the built tree to the moved positions (repeating it with the
+    # same positions leaves the same tree), then its solve
+    t_r, rebuilt = timed(lambda: h.refit(moved, m_d))
+    t_rs, _ = timed(lambda: h.accel_self(theta, eps, G, out))
+    t_rb, _ = timed(lambda: h.rebuild(moved, m_d))
+    t_rbs, _ = timed(lambda: h.accel_self(theta, eps, G, out))
+    h.close()
+    return {"workload": f"Plummer N={n:,} (seed 1), form fast: {n_targets:,} external targets "
+                        "uniform in [-5, 5]^3 (seed 5), refit after positions += 0.01 N(0,1) "
+                        "(seed 6), rebuild",
+            "targets": {"accels_per_s": n_targets / t_tg, "ms": t_tg * 1e3,
+                        "interactions": {"p2p": p2p_t, "m2p": m2p_t}},
+            "refit": {"ms": t_r * 1e3, "fell_back_to_rebuild": bool(rebuilt),
+                      "solve_ms": t_rs * 1e3},
+            "rebuild": {"ms": t_rb * 1e3, "solve_ms": t_rbs * 1e3},
+            "note": "refit and rebuild ms include the input check and error-word round trips "
+                    "to the host; medians of " + str(reps)}
+
+
 def c1_record(*, n: int = 10_000, theta: float = 0.5, eps: float = 0.01, G: float = 1.0,
               leaf: int = 32, steps: int = 50, e2e_calls: int = 20,
               fma_rate: float | None = None):
