@@ -45,6 +45,17 @@ constexpr int kFastThreads = kFastWarps * kWarp;
 #ifndef BHUT_F32_UNROLL
 #define BHUT_F32_UNROLL 8
 #endif
+// Self accelerations of few targets: up to this many lanes per target (1, 2
+// or 4; k_traverse_fast_lpt).
+#ifndef BHUT_FAST_MAX_LPT
+#define BHUT_FAST_MAX_LPT 4
+#endif
+// ... chosen so that at least this many warps per SM share the work
+#ifndef BHUT_FAST_LPT_WARPS_PER_SM
+#define BHUT_FAST_LPT_WARPS_PER_SM 8
+#endif
+static_assert(BHUT_FAST_MAX_LPT == 1 || BHUT_FAST_MAX_LPT == 2 || BHUT_FAST_MAX_LPT == 4 ||
+              BHUT_FAST_MAX_LPT == 8, "lanes per target: 1, 2, 4 or 8");
 constexpr int kFastBlocksPerSM = BHUT_FAST_BLOCKS;
 constexpr int kF32Unroll = BHUT_F32_UNROLL;
 
@@ -173,7 +184,11 @@ struct FastArgs {
 
 // SOFT_PATH (= !FAR && !CHECK): every pair is taken by pair_ff_soft (no
 // FP64 fallback); UNIT: leaf pairs skip the mass product (unit masses).
-template <int DIM, bool FAR, bool CHECK, bool UNIT = false>
+// LPT > 1 (soft path only): LPT consecutive lanes hold the same target; they
+// take the same opening decisions, share its leaf pairs (lane j of the group
+// takes pairs j, j + LPT, ...), the group's first lane alone adds monopoles
+// and counts, and the caller adds the lanes' sums.
+template <int DIM, bool FAR, bool CHECK, bool UNIT = false, int LPT = 1>
 __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const FastArgs& a,
                                      int w, int lane, bool valid, int64_t me_sorted, const float* Th,
                                      const float* Tl, float band_abs, double x, double y, double z,
@@ -181,9 +196,12 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                                      float4 (*sh)[kWarp], float4 (*sl)[kWarp],
                                      unsigned* cnt, bool& overflow)
 {
+    static_assert(LPT == 1 || (!FAR && !CHECK), "lane groups serve the soft path only");
     const unsigned FULL = 0xffffffffu;
     const float theta_f = (float)a.theta;
     const double eps2 = __dmul_rn(a.eps, a.eps);
+    const bool lead = (lane & (LPT - 1)) == 0;   // first lane of the target's group
+    const int sub = lane & (LPT - 1);
     const unsigned live = __ballot_sync(FULL, valid);
     if (lane == 0) stack[w][0] = make_int2(0, (int)live);
     int sp = 1;
@@ -194,7 +212,7 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
         const int node = e.x;
         const unsigned mask = (unsigned)e.y;
         const bool act = (mask >> lane) & 1u;
-        cnt[2] += act;
+        cnt[2] += act && lead;
         const int4 hd = ft.nhdr[node];   // (first_child, start, count, mass != 0)
         if (!hd.w) continue;              // mass == 0 skip (bh.py:514)
         const int fc = hd.x;
@@ -208,16 +226,23 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                 }
                 __syncwarp();
                 const int cn = min(kWarp, c - b);
-                if (act) {
+                if (act && lead) {
                     // The target itself (self mode: sorted index `me_sorted`)
                     // sits at zero displacement and adds exactly zero, so it
                     // is not skipped; it is only left out of the pair count
                     // (bh.py:254).
                     cnt[0] += cn - (me_sorted >= s + b && me_sorted < s + b + cn);
                 }
-                if (!FAR && !CHECK) {
+                if (!FAR && !CHECK && LPT == 1) {
                     leaf_block_soft<DIM, UNIT>(mask, lane, Th, Tl, sh[w], sl[w], cn, a.e2h, a.e2l,
                                                ah, al);
+                } else if (!FAR && !CHECK) {
+                    if (act) {
+#pragma unroll (kSplitUnroll)
+                        for (int q = sub; q < cn; q += LPT)
+                            pair_ff_soft<DIM, UNIT>(Th, Tl, sh[w][q], sl[w][q], a.e2h, a.e2l, ah,
+                                                    al);
+                    }
                 } else if (act) {
                     unsigned fb = 0;   // pairs left to FP64 (rare), taken after the loop
 #pragma unroll (kFFUnroll)
@@ -265,11 +290,11 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                     open = false;
                 } else {
                     open = open_exact64<DIM>(x, y, z, t.cm[node], t.size[node], a.theta);
-                    cnt[3]++;
+                    cnt[3] += lead;
                 }
             }
             const unsigned omask = __ballot_sync(FULL, act && open);
-            if (act && !open) {
+            if (act && !open && lead) {
                 const float4 nl = ft.nl[node];   // (cached: read by the opening test)
                 if (!FAR && !CHECK) {
                     pair_ff_soft<DIM, false>(Th, Tl, nh, nl, a.e2h, a.e2l, ah, al);
@@ -357,6 +382,78 @@ k_traverse_fast(TreeDev t, FastTree ft, FastArgs a)
             for (int k = 0; k < DIM; k++) {
                 double v = __dadd_rn((double)ah[k], (double)al[k]);
                 a.out[o * DIM + k] = __dadd_rn(__dmul_rn(v, conv), __dmul_rn(a64[k], a.G));
+            }
+        }
+    }
+}
+
+// Self accelerations of few targets (fewer warps than two per SM
+// sub-partition): LPT lanes per target, so that LPT times as many warps
+// share the work (soft path only; the group's partial sums are added by
+// shuffles in a fixed order at the end).
+template <int DIM, int LPT>
+__global__ void __launch_bounds__(kFastThreads, kFastBlocksPerSM)
+k_traverse_fast_lpt(TreeDev t, FastTree ft, FastArgs a)
+{
+    constexpr int kTargets = kWarp / LPT;   // targets per warp
+    __shared__ int2 stack[kFastWarps][kStackDepth];
+    __shared__ float4 sh[kFastWarps][kWarp], sl[kFastWarps][kWarp];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned FULL = 0xffffffffu;
+    const FastFrame fr = *ft.frame;
+    const double conv = __dmul_rn(fr.conv, a.G);
+    for (int64_t base = ((int64_t)blockIdx.x * kFastWarps + w) * kTargets; base < a.nt;
+         base += (int64_t)gridDim.x * kFastWarps * kTargets) {
+        const int64_t i = base + lane / LPT;
+        const bool valid = i < a.nt;
+        float Th[3] = {0.f, 0.f, 0.f}, Tl[3] = {0.f, 0.f, 0.f};
+        double x = 0.0, y = 0.0, z = 0.0;
+        if (valid) {
+            const float4 h = ft.ph[i], l = ft.pl[i];
+            Th[0] = h.x; Th[1] = h.y; Th[2] = h.z;
+            Tl[0] = l.x; Tl[1] = l.y; Tl[2] = l.z;
+            x = a.tx[i];
+            y = a.ty[i];
+            z = DIM == 3 ? a.tz[i] : 0.0;
+        }
+        const float band_abs = kBandAbs * 2.0f;
+        float ah[3] = {0.f, 0.f, 0.f}, al[3] = {0.f, 0.f, 0.f};
+        double a64[3] = {0.0, 0.0, 0.0};
+        unsigned cnt[5] = {0, 0, 0, 0, 0};
+        const int64_t me_sorted = valid ? i : -1;
+        bool overflow = false;
+        if (fr.unit)
+            walk<DIM, false, false, true, LPT>(t, ft, a, w, lane, valid, me_sorted, Th, Tl,
+                                               band_abs, x, y, z, ah, al, a64, stack, sh, sl, cnt,
+                                               overflow);
+        else
+            walk<DIM, false, false, false, LPT>(t, ft, a, w, lane, valid, me_sorted, Th, Tl,
+                                                band_abs, x, y, z, ah, al, a64, stack, sh, sl,
+                                                cnt, overflow);
+        if (overflow && lane == 0) atomicOr(a.err, kErrStackOverflow);
+#pragma unroll
+        for (int o = LPT / 2; o >= 1; o >>= 1) {
+#pragma unroll
+            for (int k = 0; k < DIM; k++) {
+                const float bh = __shfl_down_sync(FULL, ah[k], o);
+                const float bl = __shfl_down_sync(FULL, al[k], o);
+                ff_add(ah[k], al[k], bh, bl);
+            }
+        }
+        if (a.stats) {
+#pragma unroll
+            for (int k = 0; k < 5; k++) {
+                unsigned long long v = cnt[k];
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+                if (lane == 0 && v) atomicAdd(&a.stats[k], v);
+            }
+        }
+        if (valid && (lane & (LPT - 1)) == 0) {
+            const int64_t o = a.out_idx ? a.out_idx[i] : i;
+#pragma unroll
+            for (int k = 0; k < DIM; k++) {
+                double v = __dadd_rn((double)ah[k], (double)al[k]);
+                a.out[o * DIM + k] = __dmul_rn(v, conv);
             }
         }
     }
@@ -568,7 +665,28 @@ int launch_traverse_fast(const TreeDev& t, const FastTree& ft, const float4* th,
         else k_traverse_fp32<2><<<grid, kFastThreads, 0, s>>>(t, ft, a);
     } else {
         const bool soft = a.e2h >= 2.0f * kTinyR;
-        if (t.dim == 3) {
+        // few self targets: lanes per target so that about two warps run on
+        // each SM sub-partition (self targets lie in the box: soft path)
+        int lpt = 1;
+        if (soft && th == nullptr && BHUT_FAST_MAX_LPT > 1) {
+            int dev = 0, sms = 0;
+            BHUT_CUDA(cudaGetDevice(&dev));
+            BHUT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            const int64_t want = (int64_t)BHUT_FAST_LPT_WARPS_PER_SM * sms;
+            while (lpt < BHUT_FAST_MAX_LPT && (nt * lpt + kWarp - 1) / kWarp < want) lpt *= 2;
+        }
+        if (lpt > 1) {
+            const unsigned g = grid_for((nt * lpt + kWarp - 1) / kWarp, kFastWarps, 152u * 64u);
+            if (t.dim == 3) {
+                if (lpt == 2) k_traverse_fast_lpt<3, 2><<<g, kFastThreads, 0, s>>>(t, ft, a);
+                else if (lpt == 4) k_traverse_fast_lpt<3, 4><<<g, kFastThreads, 0, s>>>(t, ft, a);
+                else k_traverse_fast_lpt<3, 8><<<g, kFastThreads, 0, s>>>(t, ft, a);
+            } else {
+                if (lpt == 2) k_traverse_fast_lpt<2, 2><<<g, kFastThreads, 0, s>>>(t, ft, a);
+                else if (lpt == 4) k_traverse_fast_lpt<2, 4><<<g, kFastThreads, 0, s>>>(t, ft, a);
+                else k_traverse_fast_lpt<2, 8><<<g, kFastThreads, 0, s>>>(t, ft, a);
+            }
+        } else if (t.dim == 3) {
             if (soft) k_traverse_fast<3, true><<<grid, kFastThreads, 0, s>>>(t, ft, a);
             else k_traverse_fast<3, false><<<grid, kFastThreads, 0, s>>>(t, ft, a);
         } else {

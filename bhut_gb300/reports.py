@@ -545,8 +545,9 @@ def c1_record(*, n: int = 10_000, theta: float = 0.5, eps: float = 0.01, G: floa
         rec["roofline"] = {"bound": "fp32", "kernel": "k_traverse_fast",
                            "achieved": instr / t_trav / 1e12, "peak": fma_rate,
                            "unit": "T instr/s", "frac": instr / t_trav / 1e12 / fma_rate,
-                           "note": "313 warps of targets for 152 SMs: latency-bound at this "
-                                   "size (the traversal time includes the launch)"}
+                           "note": "10,000 targets at 4 lanes each (k_traverse_fast_lpt) are "
+                                   "1,250 warps for 152 SMs: latency-bound at this size (the "
+                                   "traversal time includes the launch)"}
     return rec, np.asarray(acc), (pos, m)
 
 
