@@ -703,7 +703,7 @@ def precision_record(*, n: int = 4_000_000, n_sample: int = 8192, thetas=(0.3, 0
 
 def served_record(*, count: int = 200, rate: float = 200.0, steps: int = 100, seed: int = 21,
                   server_seconds: float = 45.0, full_steps: int = 10, sample_requests: int = 40,
-                  solve_budget: int = 2_000_000, theta: float = 0.7,
+                  solve_budget: int = 1_000_000, theta: float = 0.7,
                   criterion: str = "bh_offset", multipole: str = "quad", leaf: int = 16,
                   fast_theta: float = 0.33, err_requests: int = 6,
                   hbm_budget: float = 150e9) -> dict:
