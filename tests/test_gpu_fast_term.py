@@ -82,3 +82,25 @@ def test_batched_traversal_timing_with_and_without_graph():
                 ms = sv.traverse_ms()
                 assert 0.0 < ms < 1e4, (graph, form, ms)
             sv.close()
+
+
+@pytest.mark.parametrize("n,dim,masses", [(5_000, 3, "equal"), (5_000, 3, "random"),
+                                          (20_000, 3, "random"), (7_000, 2, "equal")])
+def test_few_target_lane_groups(oracle_mod, n, dim, masses):
+    """Self solves of fewer targets than fill the GPU give each target 2 or 4
+    lanes (k_traverse_fast_lpt: 5,000 targets take 4, 20,000 take 2); the
+    lanes share the target's leaf pairs and add their sums at the end.  The
+    result must stay at the oracle's accuracy and agree with the same
+    particles evaluated as external targets (one lane per target; a
+    particle's own zero-distance pair adds exactly zero)."""
+    pos, m = workloads.gaussian(n, seed=n + dim, dim=dim)
+    if masses == "random":
+        m = np.random.default_rng(n).uniform(0.5, 1.5, n)
+    tree = bh.Tree(pos, m, dim=dim, form="fast").build()
+    a_self = tree.accelerations(theta=0.5, softening=0.01)
+    a_tgt = tree.accelerations(pos, theta=0.5, softening=0.01)
+    tree.close()
+    ot = oracle_mod.build_tree(pos, m, 32)
+    ref = oracle_mod.accelerations(ot, pos, m, theta=0.5, softening=0.01, G=1.0)
+    assert rel_l2(a_self, ref) < FAST_RTOL
+    assert rel_l2(a_self, a_tgt) < 1e-12
