@@ -37,10 +37,14 @@ constexpr int kSplitMaxK = BHUT_SPLIT_MAXK;
 constexpr int kSplitUnroll = BHUT_SPLIT_UNROLL;
 static_assert(kSplitMaxK <= 16, "a split gives every active target at least two lanes");
 
-// r^2 + eps^2 below this (normalised units) -> FP64 pair.  The coordinates
-// are represented to 2^-48, so a pair's relative error is about
-// 2^-47 / sqrt(R): at most 2^-30 on the fast path.
+// The coordinates are represented to 2^-48 (normalised units), so a pair's
+// relative error is about 2^-48 / sqrt(R), R = r^2 + eps^2.
+// Softened path: every R is at least eps^2, and the range test is compiled
+// out when (eps s)^2 >= 2 kTinyR.
 constexpr float kTinyR = 0x1p-34f;
+// Checked path (small or no softening): R below this -> FP64 pair, so a
+// float-float pair's relative error stays below 2^-35.
+constexpr float kTinyRCheck = 0x1p-26f;
 constexpr float kHugeR = 0x1p+100f;    // r^2 above this -> FP64 pair
 constexpr float kBandRel = 0x1p-18f;   // opening-test error band, relative part
 constexpr float kBandAbs = 0x1p-40f;   // ... absolute part per unit of (1 + |target|)
@@ -175,12 +179,12 @@ __device__ __forceinline__ bool pair_ff(const float* Th, const float* Tl, float4
     }
     const float Rs = __fadd_rn(s, lo);
     // |dx| <= 2 inside the box: only FAR targets can exceed kHugeR
-    const bool ok = FAR ? (Rs >= kTinyR && Rs <= kHugeR) : (!CHECK || Rs >= kTinyR);
+    const bool ok = FAR ? (Rs >= kTinyRCheck && Rs <= kHugeR) : (!CHECK || Rs >= kTinyRCheck);
     const float Rh = ok ? Rs : 1.0f;
     const float Rl = ok ? __fsub_rn(lo, __fsub_rn(Rs, s)) : 0.0f;
     // w = R^(-3/2): y ~ R^(-1/2); e = 1 - R y^2 exactly enough;
     // w = y^3 (1 - e)^(-3/2) = y^3 (1 + 3e/2 + 15e^2/8 + O(e^3))
-    const float y = rsqrt_mufu(Rh);                  // Rh >= kTinyR: normal
+    const float y = rsqrt_mufu(Rh);                  // Rh >= kTinyRCheck: normal
     const float Y = __fmul_rn(y, y);
     const float Ye = __fmaf_rn(y, y, -Y);
     const float e = -__fmaf_rn(Rh, Ye, __fmaf_rn(Rl, Y, __fmaf_rn(Rh, Y, -1.0f)));

@@ -56,6 +56,10 @@ constexpr int kFastThreads = kFastWarps * kWarp;
 #endif
 static_assert(BHUT_FAST_MAX_LPT == 1 || BHUT_FAST_MAX_LPT == 2 || BHUT_FAST_MAX_LPT == 4 ||
               BHUT_FAST_MAX_LPT == 8, "lanes per target: 1, 2, 4 or 8");
+// Checked path (small or no softening): split sparse leaf visits (1) or not.
+#ifndef BHUT_CHECK_SPLIT
+#define BHUT_CHECK_SPLIT 1
+#endif
 constexpr int kFastBlocksPerSM = BHUT_FAST_BLOCKS;
 constexpr int kF32Unroll = BHUT_F32_UNROLL;
 
@@ -182,6 +186,92 @@ struct FastArgs {
     int mac;                 // 0: reference criterion, 1: offset criterion (fp32 form)
 };
 
+// leaf_block_soft for the checked path (targets inside the box, softening
+// too small to bound r^2 + eps^2 from below: pair_ff with the range test,
+// pairs below kTinyRCheck taken in FP64 from the FP64 particle arrays).  The
+// split is the same; a lane that works for another lane's target also
+// takes that target's FP64 pairs (the target's FP64 coordinates come by
+// shuffle) and the group adds its FP64 partial sums like the float-float
+// ones.  `nfb` counts the FP64 pairs a lane evaluated.
+template <int DIM>
+__device__ __forceinline__ void leaf_block_check(unsigned mask, int lane, const float* Th,
+                                                 const float* Tl, double x, double y, double z,
+                                                 const float4* sh, const float4* sl, int cn,
+                                                 int first, const TreeDev& t, float e2h,
+                                                 float e2l, double eps2, float* ah, float* al,
+                                                 double* a64, unsigned& nfb)
+{
+    const unsigned FULL = 0xffffffffu;
+    const bool mine = (mask >> lane) & 1u;
+    const int k = __popc(mask);
+    if (k == 0) return;
+    if (k > kSplitMaxK || !BHUT_CHECK_SPLIT) {
+        if (mine) {
+            unsigned fb = 0;
+#pragma unroll (kFFUnroll)
+            for (int q = 0; q < cn; q++)
+                fb |= (unsigned)!pair_ff<DIM, false, true>(Th, Tl, sh[q], sl[q], e2h, e2l, ah,
+                                                           al) << q;
+            while (fb) {
+                const int gi = first + __ffs(fb) - 1;
+                fb &= fb - 1;
+                pair_fp64<DIM>(x, y, z, t.sx[gi], t.sy[gi], DIM == 3 ? t.sz[gi] : 0.0, t.sm[gi],
+                               eps2, a64);
+                nfb++;
+            }
+        }
+        return;
+    }
+    int f = 2;
+    while (f * 2 * k <= kWarp) f *= 2;
+    const int r = lane / f, sub = lane & (f - 1);
+    const bool work = r < k;
+    const int owner = nth_set_bit(mask, work ? r : 0);
+    float T[3] = {0.f, 0.f, 0.f}, L[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+        T[c] = __shfl_sync(FULL, Th[c], owner);
+        L[c] = __shfl_sync(FULL, Tl[c], owner);
+    }
+    const double X = __shfl_sync(FULL, x, owner), Y = __shfl_sync(FULL, y, owner);
+    const double Z = __shfl_sync(FULL, z, owner);
+    float ph[3] = {0.f, 0.f, 0.f}, pl[3] = {0.f, 0.f, 0.f};
+    double p64[3] = {0.0, 0.0, 0.0};
+    if (work) {
+        unsigned fb = 0;
+#pragma unroll (kSplitUnroll)
+        for (int q = sub; q < cn; q += f)
+            fb |= (unsigned)!pair_ff<DIM, false, true>(T, L, sh[q], sl[q], e2h, e2l, ph, pl) << q;
+        while (fb) {
+            const int gi = first + __ffs(fb) - 1;
+            fb &= fb - 1;
+            pair_fp64<DIM>(X, Y, Z, t.sx[gi], t.sy[gi], DIM == 3 ? t.sz[gi] : 0.0, t.sm[gi],
+                           eps2, p64);
+            nfb++;
+        }
+    }
+    for (int o = f >> 1; o >= 1; o >>= 1) {
+#pragma unroll
+        for (int c = 0; c < DIM; c++) {
+            const float bh = __shfl_down_sync(FULL, ph[c], o);
+            const float bl = __shfl_down_sync(FULL, pl[c], o);
+            ff_add(ph[c], pl[c], bh, bl);
+            p64[c] = __dadd_rn(p64[c], __shfl_down_sync(FULL, p64[c], o));
+        }
+    }
+    const int leader = mine ? __popc(mask & ((1u << lane) - 1u)) * f : 0;
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+        const float gh = __shfl_sync(FULL, ph[c], leader);
+        const float gl = __shfl_sync(FULL, pl[c], leader);
+        const double g64 = __shfl_sync(FULL, p64[c], leader);
+        if (mine) {
+            ff_add(ah[c], al[c], gh, gl);
+            a64[c] = __dadd_rn(a64[c], g64);
+        }
+    }
+}
+
 // SOFT_PATH (= !FAR && !CHECK): every pair is taken by pair_ff_soft (no
 // FP64 fallback); UNIT: leaf pairs skip the mass product (unit masses).
 // LPT > 1 (soft path only): LPT consecutive lanes hold the same target; they
@@ -243,6 +333,9 @@ __device__ __forceinline__ void walk(const TreeDev& t, const FastTree& ft, const
                             pair_ff_soft<DIM, UNIT>(Th, Tl, sh[w][q], sl[w][q], a.e2h, a.e2l, ah,
                                                     al);
                     }
+                } else if (!FAR) {
+                    leaf_block_check<DIM>(mask, lane, Th, Tl, x, y, z, sh[w], sl[w], cn, s + b, t,
+                                          a.e2h, a.e2l, eps2, ah, al, a64, cnt[4]);
                 } else if (act) {
                     unsigned fb = 0;   // pairs left to FP64 (rare), taken after the loop
 #pragma unroll (kFFUnroll)

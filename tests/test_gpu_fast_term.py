@@ -104,3 +104,19 @@ def test_few_target_lane_groups(oracle_mod, n, dim, masses):
     ref = oracle_mod.accelerations(ot, pos, m, theta=0.5, softening=0.01, G=1.0)
     assert rel_l2(a_self, ref) < FAST_RTOL
     assert rel_l2(a_self, a_tgt) < 1e-12
+
+
+def test_unsoftened_checked_path_against_exact():
+    """Softening 0 (the reference's default): the float-float term keeps its
+    range test, pairs closer than 2^-17 box half-sizes (and every particle's
+    own zero-distance pair) go to FP64, and sparse leaf visits are split
+    across idle lanes together with their FP64 pairs.  Against the IEEE-FP64
+    form on every target of a 200k Plummer sphere."""
+    pos, m = workloads.plummer(200_000, seed=13)
+    t = bh.Tree(pos, m, form="fast").build()
+    a = t.accelerations(theta=0.5, softening=0.0)
+    exact_dec, fp64_pairs = t._handle.fallbacks()
+    t.close()
+    ref = bh.accelerations(pos, m, theta=0.5, softening=0.0, form="exact")
+    assert fp64_pairs >= len(pos)          # at least the zero-distance pairs
+    assert rel_l2(a, ref) < 1e-10
