@@ -17,13 +17,16 @@
 //    high parts); (r^2)^(-3/2) is the hardware rsqrt refined by one
 //    correction step, w = y^3 (1 + 3e/2 + 15e^2/8) with e = 1 - r^2 y^2
 //    computed exactly (Newton-Raphson for the inverse square root, carried
-//    to second order); m * w * dx and the accumulation are float-float
-//    (Dekker/Knuth two-product and TwoSum).
-//  * Pairs with r^2 + eps^2 below 2^-34 in normalised units (softened
-//    distance under 2^-16 of the box half-size), or outside the FP32 range,
-//    are evaluated in FP64 from the FP64 arrays instead; above it a pair's
-//    relative error, dominated by the 2^-48 coordinate representation, stays
-//    below 2^-30.
+//    to second order; the softened term pair_ff_soft stops at first order);
+//    m * w * dx and the accumulation are float-float (Dekker/Knuth
+//    two-product and TwoSum).
+//  * A pair's relative error is dominated by the 2^-48 coordinate
+//    representation: about 2^-48 / sqrt(r^2 + eps^2).  With a softening
+//    that bounds r^2 + eps^2 from below ((eps s)^2 >= 2^-33) every pair is
+//    float-float and the range test is compiled out; otherwise pairs with
+//    r^2 + eps^2 below 2^-26 in normalised units (softened distance under
+//    2^-13 of the box half-size), or outside the FP32 range, are evaluated
+//    in FP64 from the FP64 arrays, so a float-float pair stays below 2^-35.
 //  * The opening decision is the reference's, bit for bit: a FP32 test
 //    decides every node whose ratio is clearly above or below theta, and
 //    nodes inside a small error band are decided by the exact FP64 test of
